@@ -1,0 +1,144 @@
+// gpurir_internal.cuh -- shared device helpers and launch descriptors of the
+// gpurir_gb300 image-source-method (ISM) engine for sm_103a.
+//
+// Reference behaviour restated here comes from src/gpuRIR_cuda.cu of gpuRIR
+// (file:line citations at each helper).  Nothing in this file is a copy of it.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpurir {
+
+// Polar patterns, numbering of src/gpuRIR_cuda.h:2-8.
+enum Pattern { P_OMNI = 0, P_HOMNI = 1, P_CARD = 2, P_HYPCARD = 3, P_SUBCARD = 4, P_BIDIR = 5 };
+
+// Maximum exponent + 1 of the per-wall reflection power tables.
+constexpr int kPowMax = 96;
+
+// One room of a launch.  Device-resident; the host fills it (ism_host.cu).
+struct RoomDesc {
+    float L[3];            // room size [m]
+    int nb[3];             // images per axis
+    int n_img;             // nb[0]*nb[1]*nb[2]
+    int n_ism;             // samples of the early (ISM) part
+    int n_total;           // samples per RIR row
+    int n_src, n_rcv;      // sources / receivers of this room
+    int src_off, rcv_off;  // first row of this room in the position arrays
+    int rir_off;           // global index of the room's first RIR (src-major)
+    int spkr, mic;         // polar patterns
+    float kh, kl;          // Fs / c as a float-float pair (samples per metre)
+    float H;               // half window Tw/2 [samples]
+    float H2;              // H*H
+    float wc[4];           // window polynomial in x^2: cos(pi x/Tw) = (H2 - x^2) * poly(x^2)
+    float T60;             // Sabine T60 of the walls (tail)
+    float fs;              // sampling rate
+    float beta[6];         // wall reflection coefficients (tail / adjoint)
+    long long out_off;     // element offset of the room's first RIR row in the output
+    int pow_n;             // valid entries per wall in the power table
+    int pad_[3];
+    float pw[6][kPowMax];  // pw[w][k] = (-beta[w])^k, rounded from FP64
+};
+
+// One work item of the persistent ISM kernel: one RIR, one segment of samples.
+struct IsmItem {
+    int room;       // index into the RoomDesc table
+    int src, rcv;   // rows of the position arrays (global)
+    int t_lo, t_hi; // output samples [t_lo, t_hi) of the early part
+    int rir;        // global RIR index
+    long long out_row;  // element offset of sample 0 of this RIR in the output
+};
+
+// ---------------------------------------------------------------------------
+// Float-float ("double-float") arithmetic from error-free transformations
+// (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2).  Used for image geometry so that
+// delays keep ~1e-10 absolute precision in samples with FP32 hardware only:
+// GB300's FP64 rate is ~1/64 of its FP32 rate.
+// ---------------------------------------------------------------------------
+struct ff { float hi, lo; };
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {  // |a| >= |b|
+    float s = __fadd_rn(a, b);
+    float e = __fsub_rn(b, __fsub_rn(s, a));
+    return {s, e};
+}
+__device__ __forceinline__ ff ff_two_prod(float a, float b) {
+    float p = __fmul_rn(a, b);
+    float e = __fmaf_rn(a, b, -p);
+    return {p, e};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    ff s = ff_two_sum(a.hi, b.hi);
+    float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return ff_fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ ff ff_sqr(ff a) {
+    ff p = ff_two_prod(a.hi, a.hi);
+    float e = __fmaf_rn(2.0f * a.hi, a.lo, p.lo);
+    return ff_fast_two_sum(p.hi, e);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    ff p = ff_two_prod(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+    return ff_fast_two_sum(p.hi, e);
+}
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+    float s = __fsqrt_rn(a.hi);
+    ff p = ff_two_prod(s, s);
+    float r = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), a.lo), 2.0f * s);
+    return ff_fast_two_sum(s, r);
+}
+
+// ---------------------------------------------------------------------------
+// Image bookkeeping of src/gpuRIR_cuda.cu:336-342: k = n - N/2,
+// clust = ceil(k/2), refl = |k mod 2|; coordinate 2*clust*L + (1-2 refl)*src.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void image_axis(int n, int N, int &clust, int &refl) {
+    int k = n - N / 2;
+    clust = (k + 1) >> 1;   // arithmetic shift: ceil(k/2) for every sign of k
+    refl = k & 1;           // |k % 2| in two's complement
+}
+
+// Directivity gain, src/gpuRIR_cuda.cu:132-147, with the cosine already formed.
+__device__ __forceinline__ float pattern_gain(float cos_t, int pattern) {
+    switch (pattern) {
+    case P_HOMNI:   return cos_t > 0.0f ? 1.0f : 0.0f;
+    case P_CARD:    return 0.5f + 0.5f * cos_t;
+    case P_HYPCARD: return 0.25f + 0.75f * cos_t;
+    case P_SUBCARD: return 0.75f + 0.25f * cos_t;
+    case P_BIDIR:   return cos_t;
+    default:        return 1.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11), the counter-based generator of the
+// diffuse tail.  Bit-exact with oracle/ism_oracle.c:orc_philox4x32_10.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Uniform in (0, 1) from the top 23 bits: (m + 0.5) * 2^-23, exact in float32.
+__device__ __forceinline__ float u01(uint32_t x) {
+    return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f;
+}
+
+// Error codes shared by kernels and host (written to a device status word).
+enum DevError : int { DEV_OK = 0, DEV_BAD_ITEM = 1, DEV_BAD_ROOM = 2 };
+
+}  // namespace gpurir

@@ -1,0 +1,115 @@
+/*
+ * gpurir_gb300.h -- C ABI of the gpurir_gb300 room-impulse-response engine
+ * (image-source method on one NVIDIA GB300, sm_103a).
+ *
+ * Plain pointers, sizes and status codes only: no C++ or torch types cross
+ * this boundary.  Every function returns GPURIR_OK (0) or a negative status;
+ * gpurir_last_error() gives a message for the calling thread.  Nothing here
+ * calls exit(), unlike the reference's gpuErrchk (src/gpuRIR_cuda.cu:68-93).
+ *
+ * A handle owns one CUDA stream, a grow-only device workspace and pinned
+ * staging memory.  A handle is not thread-safe: use one per host thread.
+ * Functions with a `stream` argument are stream-ordered on that stream
+ * (NULL means the handle's own stream) and return before the GPU finishes;
+ * the others block until their results are on the host.
+ *
+ * Array layouts are C order; positions are [count][3] float32 metres.
+ * Polar patterns: 0 omni, 1 homni, 2 card, 3 hypcard, 4 subcard, 5 bidir
+ * (src/gpuRIR_cuda.h:2-8).
+ */
+#ifndef GPURIR_GB300_H
+#define GPURIR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPURIR_OK 0
+#define GPURIR_ERR_INVALID (-1)   /* bad argument: sizes, patterns, lengths */
+#define GPURIR_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define GPURIR_ERR_DEVICE (-3)    /* a kernel reported an inconsistent work item */
+#define GPURIR_ERR_UNSUPPORTED (-4)
+
+#define GPURIR_NOISE_LOGISTIC 0   /* the reference's transform, src/gpuRIR_cuda.cu:454-455 */
+#define GPURIR_NOISE_GAUSSIAN 1   /* Box-Muller on the same Philox words */
+
+typedef struct gpurir_sim gpurir_sim;
+
+/* Version string of the library. */
+const char *gpurir_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char *gpurir_last_error(void);
+
+/* Create a simulator on the current CUDA device.
+ * Replaces gpuRIR_cuda::gpuRIR_cuda(bool, bool), src/gpuRIR_cuda.cu:1025-1048
+ * (flags as the Python binding's default, src/python_bind.cpp:15).
+ * The tail noise is keyed by `seed` (the reference fixes cuRAND's seed to 1234,
+ * src/gpuRIR_cuda.cu:1046-1047); every simulate call advances a call counter so
+ * successive calls draw different noise, as the stateful generator does. */
+int gpurir_create(int mixed_precision, int lookup_table, uint64_t seed, gpurir_sim **out);
+
+/* Release a simulator and its workspace. */
+int gpurir_destroy(gpurir_sim *sim);
+
+/* Mode flags.  Replace gpuRIR_cuda::activate_mixed_precision / activate_lut,
+ * src/gpuRIR_cuda.cu:1050-1073: the two modes exclude each other, turning one
+ * on turns the other off.  *state receives the resulting flag (may be NULL). */
+int gpurir_activate_mixed_precision(gpurir_sim *sim, int activate, int *state);
+int gpurir_activate_lut(gpurir_sim *sim, int activate, int *state);
+
+/* Read the flags. */
+int gpurir_get_modes(gpurir_sim *sim, int *mixed_precision, int *lookup_table);
+
+/* Noise transform of the tail (GPURIR_NOISE_*), and the (seed, call counter)
+ * pair that keys it.  The counter advances by one per simulate call. */
+int gpurir_set_noise(gpurir_sim *sim, int noise_kind);
+int gpurir_set_seed(gpurir_sim *sim, uint64_t seed, uint64_t call_counter);
+int gpurir_get_seed(gpurir_sim *sim, uint64_t *seed, uint64_t *call_counter);
+
+/* Number of samples for a duration: ceil(T*Fs) in float32, rounded up to even
+ * (src/gpuRIR_cuda.cu:831-835, src/python_bind.cpp:82-83). */
+int gpurir_n_samples(float T, float Fs);
+
+/*
+ * Simulate the RIRs of one room, host buffers in and out.
+ * Replaces gpuRIR_cuda::cuda_simulateRIR, src/gpuRIR_cuda.cu:766-931, called
+ * by gpuRIR_bind::simulateRIR_bind, src/python_bind.cpp:29-88.  Same argument
+ * order and meaning; the caller owns `rir_out`, a float32 buffer of
+ * M_src * M_rcv * gpurir_n_samples(Tmax, Fs) values laid out
+ * [M_src][M_rcv][nSamples] (the reference malloc()s it and returns it).
+ * orV_src / orV_rcv may be NULL for omni patterns.
+ */
+int gpurir_simulate_rir(gpurir_sim *sim, const float room_sz[3], const float beta[6],
+                        const float *pos_src, int M_src, const float *pos_rcv,
+                        const float *orV_src, const float *orV_rcv, int spkr_pattern,
+                        int mic_pattern, int M_rcv, const int nb_img[3], float Tdiff,
+                        float Tmax, float Fs, float c, float *rir_out);
+
+/* Same computation with device pointers, stream-ordered: positions and
+ * orientations on the device, `d_rir_out` a device buffer of the same shape.
+ * No host synchronisation. */
+int gpurir_simulate_rir_device(gpurir_sim *sim, const float room_sz[3], const float beta[6],
+                               const float *d_pos_src, int M_src, const float *d_pos_rcv,
+                               const float *d_orV_src, const float *d_orV_rcv, int spkr_pattern,
+                               int mic_pattern, int M_rcv, const int nb_img[3], float Tdiff,
+                               float Tmax, float Fs, float c, float *d_rir_out, void *stream);
+
+/* Raw Philox4x32-10 words of the tail stream of one RIR (counter blocks
+ * (j, rir_index, call_lo, call_hi), key (seed_lo, seed_hi)), into device
+ * memory; for checking the stream bit-exactly against a host replay. */
+int gpurir_philox_stream_device(uint64_t seed, uint64_t call_counter, uint32_t rir_index,
+                                long n_words, uint32_t *d_out, void *stream);
+
+/* Envelope of the last simulate call on this handle: per RIR (A, alpha, tau_dp)
+ * as the tail used them (src/gpuRIR_cuda.cu:415-443).  `out` holds 3*n floats. */
+int gpurir_last_envelope(gpurir_sim *sim, float *out, long n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPURIR_GB300_H */

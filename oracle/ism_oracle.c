@@ -1,0 +1,357 @@
+/*
+ * ism_oracle.c -- CPU restatement of gpuRIR's image-source-method (ISM) pipeline.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA path
+ * in gpurir_gb300/csrc.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it.  The product never links it or falls back to it.
+ *
+ * Parity status of this restatement:
+ *   - The host-side helpers and the trajectory overlap-add it is used with are
+ *     pinned against golden vectors produced by importing the reference's own
+ *     Python package (tests/golden/make_golden.py).
+ *   - The CUDA kernels of the reference (src/gpuRIR_cuda.cu) cannot be executed
+ *     in the build container (no GPU) nor on the GPU host (the reference sources
+ *     are not present there), so the ISM arithmetic below is PARITY UNPINNED
+ *     against a run of the reference; it is a line-by-line restatement of the
+ *     formulas cited below, checked by hand-derived known answers in tests/.
+ *
+ * Every function names the reference lines (path:line inside the gpuRIR
+ * project) that it restates.  Arithmetic is FP64 unless the name says f32.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_PI 3.14159265358979323846
+
+/* Polar patterns, src/gpuRIR_cuda.h:2-8. */
+enum { P_OMNI = 0, P_HOMNI = 1, P_CARD = 2, P_HYPCARD = 3, P_SUBCARD = 4, P_BIDIR = 5 };
+
+/* ---------------------------------------------------------------------------
+ * Lengths.  src/gpuRIR_cuda.cu:831-835 and src/python_bind.cpp:82-83 compute
+ * ceil(T*Fs) from float32 operands, then round up to an even count.
+ * ------------------------------------------------------------------------- */
+int orc_n_samples(float T, float Fs)
+{
+    float p = T * Fs;               /* float32 product, as in the reference */
+    int n = (int)ceilf(p);
+    n += n % 2;
+    return n;
+}
+
+/* Window length in samples: (int)round(8e-3f*Fs), src/gpuRIR_cuda.cu:629. */
+int orc_window_len(float Fs)
+{
+    float p = 8e-3f * Fs;
+    return (int)roundf(p);
+}
+
+/* src/gpuRIR_cuda.cu:132-147 (directivity), evaluated in FP64. */
+static double orc_directivity(const double doa[3], const double orv[3], int pattern)
+{
+    if (pattern == P_OMNI) return 1.0;
+    double c = doa[0] * orv[0] + doa[1] * orv[1] + doa[2] * orv[2];
+    c /= sqrt(doa[0] * doa[0] + doa[1] * doa[1] + doa[2] * doa[2]);
+    c /= sqrt(orv[0] * orv[0] + orv[1] * orv[1] + orv[2] * orv[2]);
+    switch (pattern) {
+    case P_HOMNI:   return c > 0.0 ? 1.0 : 0.0;
+    case P_CARD:    return 0.5 + 0.5 * c;
+    case P_HYPCARD: return 0.25 + 0.75 * c;
+    case P_SUBCARD: return 0.75 + 0.25 * c;
+    case P_BIDIR:   return c;
+    default:        return 0.0;
+    }
+}
+
+/* Per-axis image bookkeeping of src/gpuRIR_cuda.cu:336-342:
+ *   k = n - N/2, clust = ceil(k/2), r = |k mod 2| (C remainder). */
+static void orc_axis(int n, int N, int *clust, int *refl)
+{
+    int k = n - N / 2;
+    *clust = (int)ceil(k / 2.0);
+    *refl = abs(k % 2);
+}
+
+/*
+ * Amplitude and delay (in samples) of every image for every (src, rcv) pair.
+ * Restates calcAmpTau_kernel, src/gpuRIR_cuda.cu:245-375.
+ *   amp, tau : [M_src][M_rcv][N0*N1*N2], image index n0*N1*N2 + n1*N2 + n2
+ *   tau_dp   : [M_src][M_rcv], delay of the direct path (all clust = refl = 0)
+ */
+void orc_amp_tau(const float room[3], const float beta[6],
+                 const float *pos_src, int M_src, const float *pos_rcv, int M_rcv,
+                 const float *orv_src, const float *orv_rcv, int spkr_pattern, int mic_pattern,
+                 const int nb_img[3], float c, float Fs,
+                 double *amp, double *tau, double *tau_dp)
+{
+    const int N0 = nb_img[0], N1 = nb_img[1], N2 = nb_img[2];
+    const long NN = (long)N0 * N1 * N2;
+    for (int n0 = 0; n0 < N0; n0++)
+    for (int n1 = 0; n1 < N1; n1++)
+    for (int n2 = 0; n2 < N2; n2++) {
+        int n[3] = {n0, n1, n2}, N[3] = {N0, N1, N2};
+        int clust[3], refl[3];
+        double att = 1.0;
+        int direct = 1;
+        for (int d = 0; d < 3; d++) {
+            orc_axis(n[d], N[d], &clust[d], &refl[d]);
+            /* beta is negated before the powers, src/gpuRIR_cuda.cu:272-277, 340 */
+            att *= pow(-(double)beta[2 * d], abs(clust[d] - refl[d])) *
+                   pow(-(double)beta[2 * d + 1], abs(clust[d]));
+            direct = direct && clust[d] == 0 && refl[d] == 0;
+        }
+        long idx = (long)n0 * N1 * N2 + (long)n1 * N2 + n2;
+        for (int ms = 0; ms < M_src; ms++)
+        for (int mr = 0; mr < M_rcv; mr++) {
+            double vec[3], im2rcv[3], osrc[3], dist2 = 0.0;
+            for (int d = 0; d < 3; d++) {
+                double s = (1 - 2 * refl[d]);
+                /* vector from the receiver to the image, src/gpuRIR_cuda.cu:353 */
+                vec[d] = clust[d] * 2.0 * (double)room[d] + s * (double)pos_src[ms * 3 + d]
+                         - (double)pos_rcv[mr * 3 + d];
+                dist2 += vec[d] * vec[d];
+                osrc[d] = s * (double)orv_src[ms * 3 + d];   /* mirrored source axis, :357 */
+                im2rcv[d] = -vec[d];
+            }
+            double dist = sqrt(dist2);
+            double a = att / (4.0 * ORC_PI * dist);
+            if (spkr_pattern != P_OMNI) a *= orc_directivity(im2rcv, osrc, spkr_pattern);
+            if (mic_pattern != P_OMNI) {
+                double orc[3] = {orv_rcv[mr * 3], orv_rcv[mr * 3 + 1], orv_rcv[mr * 3 + 2]};
+                a *= orc_directivity(vec, orc, mic_pattern);
+            }
+            long o = ((long)ms * M_rcv + mr) * NN + idx;
+            amp[o] = a;
+            tau[o] = dist / (double)c * (double)Fs;
+            if (direct) tau_dp[ms * M_rcv + mr] = tau[o];
+        }
+    }
+}
+
+/*
+ * Windowed-sinc accumulation of the early part.  Restates image_sample,
+ * hanning_window and sinc (src/gpuRIR_cuda.cu:110-121) summed over images as
+ * generateRIR_kernel/reduceRIR_kernel do (:377-413).  Terms outside
+ * |t - tau| < Tw/2 are exactly zero in the reference, so visiting only the
+ * window gives the same sum.
+ *   rir : [M][ld] doubles, columns [0, nISM) written (zeroed first)
+ */
+void orc_ism_sum(const double *amp, const double *tau, long M, long N, int nISM, float Fs,
+                 double *rir, long ld)
+{
+    const double Tw = (double)orc_window_len(Fs);
+    const double H = Tw / 2.0;
+    for (long m = 0; m < M; m++) {
+        double *h = rir + m * ld;
+        for (int t = 0; t < nISM; t++) h[t] = 0.0;
+        for (long i = 0; i < N; i++) {
+            double a = amp[m * N + i], ta = tau[m * N + i];
+            long t0 = (long)floor(ta - H);
+            if (t0 < 0) t0 = 0;
+            for (long t = t0; t < nISM && (double)t < ta + H; t++) {
+                double x = (double)t - ta;
+                if (fabs(x) >= H) continue;
+                double w = 0.5 * (1.0 + cos(2.0 * ORC_PI * x / Tw));
+                double s = (x == 0.0) ? 1.0 : sin(ORC_PI * x) / (ORC_PI * x);
+                h[t] += w * a * s;
+            }
+        }
+    }
+}
+
+/* Sabine reverberation time from the walls, src/gpuRIR_cuda.cu:123-130. */
+double orc_sabine_t60(const float room[3], const float beta[6])
+{
+    double b[6];
+    for (int i = 0; i < 6; i++) b[i] = beta[i];
+    double Sa = ((1 - b[0] * b[0]) + (1 - b[1] * b[1])) * room[1] * room[2] +
+                ((1 - b[2] * b[2]) + (1 - b[3] * b[3])) * room[0] * room[2] +
+                ((1 - b[4] * b[4]) + (1 - b[5] * b[5])) * room[0] * room[1];
+    double V = (double)room[0] * room[1] * room[2];
+    return 0.161 * V / Sa;
+}
+
+/*
+ * Diffuse-tail envelope, restating envPred_kernel (src/gpuRIR_cuda.cu:415-443):
+ * mean power of the last <=10 ms of the early part after the direct path, an
+ * exponential decay alpha from the Sabine T60, and the gain A that makes
+ * A*exp(alpha*(t - tau_dp)) pass through that power at the window centre.
+ * When the window is empty (tau_dp >= nISM) the reference divides by <= 0;
+ * here A is set to 0 (no tail), the documented deviation of this engine.
+ */
+void orc_env_pred(const double *rir, long ld, const double *tau_dp, long M, int nISM, float Fs,
+                  const float room[3], const float beta[6], double *A, double *alpha)
+{
+    double w_sz = (double)(10e-3f * Fs);
+    double T60 = orc_sabine_t60(room, beta);
+    double al = -13.8155 / (T60 * (double)Fs);
+    for (long m = 0; m < M; m++) {
+        double lo = (double)nISM - w_sz;
+        if (tau_dp[m] > lo) lo = tau_dp[m];
+        long ws = (long)ceil(lo);
+        alpha[m] = al;
+        if (ws >= nISM) { A[m] = 0.0; continue; }
+        double wc = ws + (nISM - ws) / 2.0;
+        double p = 0.0;
+        for (long t = ws; t < nISM; t++) p += rir[m * ld + t] * rir[m * ld + t];
+        p /= (double)(nISM - ws);
+        A[m] = p / exp(al * (wc - tau_dp[m]));
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+ * as 1, 2, 3", SC'11).  Host replay of the counter-based stream that the tail
+ * kernel uses in place of the reference's stateful cuRAND generator
+ * (src/gpuRIR_cuda.cu:874, 1046-1047).
+ * ------------------------------------------------------------------------- */
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* Raw stream of the tail for one RIR: words [0, n) of the blocks
+ * ctr = (j, rir_index, offset_lo, offset_hi), key = (seed_lo, seed_hi). */
+void orc_tail_stream(uint64_t seed, uint64_t offset, uint32_t rir_index, long n, uint32_t *out)
+{
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (long j = 0; 4 * j < n; j++) {
+        uint32_t ctr[4] = {(uint32_t)j, rir_index, (uint32_t)offset, (uint32_t)(offset >> 32)};
+        uint32_t r[4];
+        orc_philox4x32_10(ctr, key, r);
+        for (int q = 0; q < 4 && 4 * j + q < n; q++) out[4 * j + q] = r[q];
+    }
+}
+
+/* Uniform in (0, 1) from the top 23 bits of one word: (m + 0.5) * 2^-23, a
+ * value that float32 represents exactly. */
+static double orc_u01(uint32_t x) { return ((double)(x >> 9) + 0.5) * (1.0 / 8388608.0); }
+
+/*
+ * Diffuse tail, restating diffRev_kernel (src/gpuRIR_cuda.cu:445-461): unit
+ * variance noise shaped by sqrt(A*exp(alpha*(nISM + s - tau_dp))).
+ * noise_kind 0: the reference's logistic transform 0.551329*log(u/(1-u+1e-6)).
+ * noise_kind 1: Gaussian by Box-Muller on the word pairs (2j, 2j+1).
+ *   out : [M][ld], columns [nISM, nISM + nDiff) written.
+ */
+void orc_tail(const double *A, const double *alpha, const double *tau_dp, long M, int nISM, int nDiff,
+              uint64_t seed, uint64_t offset, const uint32_t *rir_index, int noise_kind,
+              double *out, long ld)
+{
+    long nw = ((long)nDiff + 3) / 4 * 4;    /* whole Philox blocks */
+    uint32_t *w = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nw + 4));
+    for (long m = 0; m < M; m++) {
+        orc_tail_stream(seed, offset, rir_index ? rir_index[m] : (uint32_t)m, nw, w);
+        for (int s = 0; s < nDiff; s++) {
+            double z;
+            if (noise_kind == 0) {
+                double u = orc_u01(w[s]);
+                z = 0.551329 * log(u / (1.0 - u + 1e-6));
+            } else {
+                int s0 = s & ~1;
+                double u1 = orc_u01(w[s0]), u2 = orc_u01(w[s0 + 1]);
+                double r = sqrt(-2.0 * log(u1));
+                z = (s & 1) ? r * sin(2.0 * ORC_PI * u2) : r * cos(2.0 * ORC_PI * u2);
+            }
+            double env = A[m] * exp(alpha[m] * ((double)nISM + s - tau_dp[m]));
+            out[m * ld + nISM + s] = sqrt(env) * z;
+        }
+    }
+    free(w);
+}
+
+/* ---------------------------------------------------------------------------
+ * FP32 CPU port: the same windowed ISM in float32 with the reference's float
+ * formulas (powf, sqrtf, cosf, sinf), threaded with OpenMP over RIRs.  This is
+ * the timed CPU baseline; it is not an accuracy reference.
+ * ------------------------------------------------------------------------- */
+static float orc_directivity_f(const float doa[3], const float orv[3], int pattern)
+{
+    if (pattern == P_OMNI) return 1.0f;
+    float c = doa[0] * orv[0] + doa[1] * orv[1] + doa[2] * orv[2];
+    c /= sqrtf(doa[0] * doa[0] + doa[1] * doa[1] + doa[2] * doa[2]);
+    c /= sqrtf(orv[0] * orv[0] + orv[1] * orv[1] + orv[2] * orv[2]);
+    switch (pattern) {
+    case P_HOMNI:   return c > 0.0f ? 1.0f : 0.0f;
+    case P_CARD:    return 0.5f + 0.5f * c;
+    case P_HYPCARD: return 0.25f + 0.75f * c;
+    case P_SUBCARD: return 0.75f + 0.25f * c;
+    case P_BIDIR:   return c;
+    default:        return 0.0f;
+    }
+}
+
+/* rir : [M_src*M_rcv][ld] floats, columns [0, nISM) written.  Returns the
+ * number of windowed image-sample updates performed. */
+long long orc_ism_f32(const float room[3], const float beta[6],
+                      const float *pos_src, int M_src, const float *pos_rcv, int M_rcv,
+                      const float *orv_src, const float *orv_rcv, int spkr_pattern, int mic_pattern,
+                      const int nb_img[3], float c, float Fs, int nISM, float *rir, long ld,
+                      int n_threads)
+{
+    const int N0 = nb_img[0], N1 = nb_img[1], N2 = nb_img[2];
+    const float PIf = 3.141592654f;
+    const float Tw = (float)orc_window_len(Fs);
+    const float H = Tw / 2.0f;
+    const long M = (long)M_src * M_rcv;
+    long long updates = 0;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : updates)
+#endif
+    for (long m = 0; m < M; m++) {
+        int ms = (int)(m / M_rcv), mr = (int)(m % M_rcv);
+        float *h = rir + m * ld;
+        for (int t = 0; t < nISM; t++) h[t] = 0.0f;
+        for (int n0 = 0; n0 < N0; n0++)
+        for (int n1 = 0; n1 < N1; n1++)
+        for (int n2 = 0; n2 < N2; n2++) {
+            int n[3] = {n0, n1, n2}, N[3] = {N0, N1, N2};
+            float att = 1.0f, vec[3], im2rcv[3], osrc[3], dist2 = 0.0f;
+            for (int d = 0; d < 3; d++) {
+                int cl, rf;
+                orc_axis(n[d], N[d], &cl, &rf);
+                att *= powf(-beta[2 * d], (float)abs(cl - rf)) * powf(-beta[2 * d + 1], (float)abs(cl));
+                vec[d] = cl * 2 * room[d] + (1 - 2 * rf) * pos_src[ms * 3 + d] - pos_rcv[mr * 3 + d];
+                dist2 += vec[d] * vec[d];
+                osrc[d] = (1 - 2 * rf) * orv_src[ms * 3 + d];
+                im2rcv[d] = -vec[d];
+            }
+            float dist = sqrtf(dist2);
+            float a = att / (4 * PIf * dist);
+            if (spkr_pattern != P_OMNI) a *= orc_directivity_f(im2rcv, osrc, spkr_pattern);
+            if (mic_pattern != P_OMNI) a *= orc_directivity_f(vec, &orv_rcv[mr * 3], mic_pattern);
+            float ta = dist / c * Fs;
+            long t0 = (long)floorf(ta - H);
+            if (t0 < 0) t0 = 0;
+            for (long t = t0; t < nISM && (float)t < ta + H; t++) {
+                float x = (float)t - ta;
+                if (fabsf(x) >= H) continue;
+                float w = 0.5f * (1.0f + cosf(2.0f * PIf * x / Tw));
+                float xs = x * PIf;
+                float s = (xs == 0.0f) ? 1.0f : sinf(xs) / xs;
+                h[t] += w * a * s;
+                updates++;
+            }
+        }
+    }
+    return updates;
+}
