@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the gpurir_gb300 forward path on one or more GB300s.
+
+One step = one simulateRIR of the mic_array workload: 64 omni sources x 32
+cardioid receivers in a 6 x 5 x 3 m room, Sabine beta at T60 = 1 s, early part
+by the ISM up to Tdiff = 0.3 s (nb_img [12, 14, 24]), Gaussian diffuse tail up
+to Tmax = 1 s, fs = 16 kHz, FP32: 2048 RIRs of 16000 samples per step.
+
+  value  RIRs/s with inputs resident in HBM (device entry of the C ABI),
+         device time from CUDA events on the launch stream, L2 flushed
+         (256 MiB write) before every timed step, max over ranks.
+  e2e    the same metric through the host entry of the C ABI
+         (gpurir_simulate_rir): positions from host memory, RIRs returned into
+         pinned host memory, both copies inside the timed region.
+
+--impl reference times the CPU restatement of the path (FP32, all host
+threads) on a bounded sample of the same workload: the reference library has
+no CPU implementation and its CUDA build cannot run here.
+Multi-GPU: every rank simulates its own copy of the workload (independent
+RIRs, no collective on the data path): weak scaling.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = ("RIRs/s & image-sample updates/s, batched vs plain fwd; fwd+adjoint step time, 1 GB300")
+WORKLOAD = "mic_array"
+WORKLOAD_DESC = ("mic_array: room 6x5x3 m, Sabine beta (T60 1.0 s), 64 omni src x 32 cardioid rcv, "
+                 "nb_img [12,14,24], Tdiff 0.3 s, Tmax 1.0 s, fs 16 kHz, Gaussian tail, FP32")
+FLOPS_PER_UPDATE = 8      # FP32 ops per windowed update of the reference formula
+SFU_PER_UPDATE = 3        # transcendental ops (sin, cos, reciprocal) per update
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _cpu_port_sample(scene, n_src, threads):
+    """RIRs/s of the FP32 CPU restatement of the early part on `n_src` sources."""
+    import oracle
+    t = time.perf_counter()
+    out, upd = oracle.ism_f32(scene["room_sz"], scene["beta"], scene["pos_src"][:n_src],
+                              scene["pos_rcv"], scene["nb_img"], scene["Tdiff"], scene["fs"],
+                              scene["spkr_pattern"], scene["mic_pattern"], None,
+                              scene["orV_rcv"], scene["c"], n_threads=threads)
+    dt = time.perf_counter() - t
+    return n_src * scene["pos_rcv"].shape[0], upd, dt
+
+
+def run_reference(a):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    from gpurir_gb300 import workloads
+    scene = workloads.mic_array()
+    threads = os.cpu_count() or 1
+    n_src = 4
+    for _ in range(max(a.warmup, 1)):
+        _cpu_port_sample(scene, n_src, threads)
+    times, n_rir, upd = [], 0, 0
+    for _ in range(a.steps):
+        n_rir, upd, dt = _cpu_port_sample(scene, n_src, threads)
+        times.append(dt)
+    step_s = sum(times) / len(times)
+    value = n_rir / step_s
+    sample = "%d of 64 sources x 32 receivers (%d RIRs) per step, early part only" % (n_src, n_rir)
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "RIRs/s", "n_gpus": 0,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD_DESC},
+            "updates_per_s": upd / step_s,
+            "cpu_baseline": {"value": value, "unit": "RIRs/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "RIRs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the ISM path (OpenMP, FP32): the reference has no CPU "
+                    "implementation and its CUDA build cannot run in this environment"}
+    print(json.dumps(line), flush=True)
+
+
+def _traffic(workload):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def run_gpu(a):
+    import torch
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import gpurir_gb300 as G
+    from gpurir_gb300 import workloads
+    scene = workloads.mic_array()
+    sp, mp = G.polar_patterns[scene["spkr_pattern"]], G.polar_patterns[scene["mic_pattern"]]
+    ms, mr = scene["pos_src"].shape[0], scene["pos_rcv"].shape[0]
+    M = ms * mr
+    ns = workloads.n_samples(scene["Tmax"], scene["fs"])
+    sim = G.Simulator(seed=1234 + rank)
+    sim.set_noise(scene["noise"])
+    sim.set_profiling(True)
+    dev = torch.device("cuda", local)
+    d_ps = torch.from_numpy(scene["pos_src"]).to(dev)
+    d_pr = torch.from_numpy(scene["pos_rcv"]).to(dev)
+    d_or = torch.from_numpy(scene["orV_rcv"]).to(dev)
+    d_out = torch.empty((ms, mr, ns), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        sim.simulate_rir_device(scene["room_sz"], scene["beta"], d_ps, d_pr, None, d_or, sp, mp,
+                                scene["nb_img"], scene["Tdiff"], scene["Tmax"], scene["fs"],
+                                scene["c"], d_out, stream.cuda_stream)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    fp32_flops, mufu_ops = G.probe_peaks()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    total_ms, ism_ms, tail_ms = 0.0, [], []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(a.steps):
+        flush.zero_()
+        ev0.record(stream)
+        step()
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+        i_ms, t_ms = sim.last_timing()
+        ism_ms.append(i_ms)
+        tail_ms.append(t_ms)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    clk = clocks.stop()
+    ms_per_step = total_ms / a.steps
+    value = world * M * a.steps / (total_ms * 1e-3)
+
+    # end to end through the host entry (positions from host memory, RIRs to pinned memory)
+    h_out = torch.empty((ms, mr, ns), dtype=torch.float32, pin_memory=True).numpy()
+
+    def host_step():
+        sim.simulate_rir(scene["room_sz"], scene["beta"], scene["pos_src"], scene["pos_rcv"],
+                         None, scene["orV_rcv"], sp, mp, scene["nb_img"], scene["Tdiff"],
+                         scene["Tmax"], scene["fs"], scene["c"], out=h_out)
+
+    for _ in range(max(2, a.warmup // 2)):
+        host_step()
+    e2e_s = 0.0
+    for _ in range(a.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_step()
+        e2e_s += time.perf_counter() - t0
+    h2d, d2h = sim.last_transfer_bytes()
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * M * a.steps / e2e_s
+
+    if rank != 0:
+        return
+    updates, brute = workloads.windowed_updates(scene)
+    ism_avg = sum(ism_ms) / len(ism_ms)
+    upd_per_s = updates / (ism_avg * 1e-3)
+    sfu_ach = upd_per_s * SFU_PER_UPDATE
+    fp32_ach = upd_per_s * FLOPS_PER_UPDATE
+    frac_sfu = sfu_ach / mufu_ops
+    frac_fp32 = fp32_ach / (fp32_flops / 2.0)
+    use_sfu = frac_sfu >= frac_fp32
+    traffic = _traffic(WORKLOAD)
+    roofline = {
+        "bound": "sfu" if use_sfu else "fp32",
+        "achieved": (sfu_ach if use_sfu else fp32_ach) / 1e12,
+        "peak": (mufu_ops if use_sfu else fp32_flops / 2.0) / 1e12,
+        "unit": "Tops/s",
+        "frac": frac_sfu if use_sfu else frac_fp32,
+        "traffic": traffic,
+        "kernel": "ism_forward_kernel<4>",
+        "basis": "%d transcendental + %d FP32 ops per windowed image-sample update; %d updates "
+                 "per launch; peaks measured on this device (MUFU rcp, FP32 FMA)" %
+                 (SFU_PER_UPDATE, FLOPS_PER_UPDATE, updates),
+        "frac_fp32": frac_fp32, "frac_sfu": frac_sfu,
+        "peak_fp32_tflops_measured": fp32_flops / 1e12, "peak_mufu_tops_measured": mufu_ops / 1e12,
+        "ism_ms": ism_avg,
+    }
+    line = {"metric": METRIC, "value": value, "unit": "RIRs/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD_DESC, "rirs_per_step": M, "samples_per_rir": ns,
+                       "windowed_updates_per_step": updates, "brute_force_evaluations": brute,
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "updates_per_s": updates * world * a.steps / (total_ms * 1e-3),
+            "kernel_ms": {"ism_forward": ism_avg, "tail": sum(tail_ms) / len(tail_ms)},
+            "e2e": {"value": e2e_value, "unit": "RIRs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3},
+            "roofline": roofline, "clocks": clk, "gpu_launches": 2 * a.steps}
+    if world == 1 and not a.no_cpu_baseline:
+        scene_cpu = workloads.mic_array()
+        threads = os.cpu_count() or 1
+        n_rir, upd, dt = _cpu_port_sample(scene_cpu, 16, threads)
+        line["cpu_baseline"] = {"value": n_rir / dt, "unit": "RIRs/s", "cores": threads,
+                                "kind": "port", "updates_per_s": upd / dt,
+                                "sample": "16 of 64 sources x 32 receivers (%d RIRs), early part, "
+                                          "FP32 OpenMP restatement" % n_rir}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1 and a.impl != "reference":
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -160,7 +160,13 @@ class Simulator:
         room = np.ascontiguousarray(np.asarray(room_sz, dtype=np.float32).reshape(3))
         b = np.ascontiguousarray(np.asarray(beta, dtype=np.float32).reshape(6))
         nb = np.ascontiguousarray(np.asarray(nb_img, dtype=np.int32).reshape(3))
+        f32 = lambda a: None if a is None else \
+            np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, 3))
+        pos_src, pos_rcv, orV_src, orV_rcv = f32(pos_src), f32(pos_rcv), f32(orV_src), f32(orV_rcv)
         ms, mr = pos_src.shape[0], pos_rcv.shape[0]
+        if (orV_src is not None and orV_src.shape[0] != ms) or \
+                (orV_rcv is not None and orV_rcv.shape[0] != mr):
+            raise ValueError("orientations must have the shape of the positions")
         ns = self._L.gpurir_n_samples(float(Tmax), float(fs))
         if out is None:
             out = np.empty((ms, mr, ns), dtype=np.float32)
@@ -174,11 +180,59 @@ class Simulator:
             float(fs), float(c), out.ctypes.data), "gpurir_simulate_rir")
         return out
 
+    def simulate_rir_device(self, room_sz, beta, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, spkr,
+                            mic, nb_img, Tdiff, Tmax, fs, c, d_out, stream=None):
+        """Stream-ordered call on device memory (torch CUDA tensors, float32, C order)."""
+        room = np.ascontiguousarray(np.asarray(room_sz, dtype=np.float32).reshape(3))
+        b = np.ascontiguousarray(np.asarray(beta, dtype=np.float32).reshape(6))
+        nb = np.ascontiguousarray(np.asarray(nb_img, dtype=np.int32).reshape(3))
+        for t in (d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_out):
+            if t is not None and (not t.is_cuda or not t.is_contiguous() or t.dtype != _torch().float32):
+                raise ValueError("device arrays must be contiguous float32 CUDA tensors")
+        if stream is None:
+            stream = _torch().cuda.current_stream().cuda_stream
+        _lib.check(self._L.gpurir_simulate_rir_device(
+            self._h, room.ctypes.data_as(_lib.fptr), b.ctypes.data_as(_lib.fptr),
+            d_pos_src.data_ptr(), d_pos_src.shape[0], d_pos_rcv.data_ptr(),
+            d_orV_src.data_ptr() if d_orV_src is not None else None,
+            d_orV_rcv.data_ptr() if d_orV_rcv is not None else None, int(spkr), int(mic),
+            d_pos_rcv.shape[0], nb.ctypes.data_as(_lib.iptr), float(Tdiff), float(Tmax), float(fs),
+            float(c), d_out.data_ptr(), ctypes.c_void_p(stream)), "gpurir_simulate_rir_device")
+        return d_out
+
+    def set_profiling(self, on=True):
+        _lib.check(self._L.gpurir_set_profiling(self._h, int(bool(on))), "set_profiling")
+
+    def last_timing(self):
+        """(ism_ms, tail_ms) of the last call, from CUDA events on its stream."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _lib.check(self._L.gpurir_last_timing(self._h, ctypes.byref(a), ctypes.byref(b)), "timing")
+        return a.value, b.value
+
+    def last_transfer_bytes(self):
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(self._L.gpurir_last_transfer_bytes(self._h, ctypes.byref(a), ctypes.byref(b)),
+                   "transfer_bytes")
+        return a.value, b.value
+
     def last_envelope(self, n):
         out = np.zeros((n, 3), dtype=np.float32)
         _lib.check(self._L.gpurir_last_envelope(self._h, out.ctypes.data_as(_lib.fptr), n),
                    "last_envelope")
         return out
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def probe_peaks():
+    """Measured FP32 FLOP/s and MUFU op/s of the current device."""
+    L = _lib.load()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _lib.check(L.gpurir_probe_peaks(ctypes.byref(a), ctypes.byref(b)), "probe_peaks")
+    return a.value, b.value
 
 
 _sim = None

@@ -42,6 +42,10 @@ SIGNATURES = {
                                            c_void_p]),
     "gpurir_philox_stream_device": (c_int, [c_u64, c_u64, c_u32, c_long, c_void_p, c_void_p]),
     "gpurir_last_envelope": (c_int, [c_void_p, fptr, c_long]),
+    "gpurir_set_profiling": (c_int, [c_void_p, c_int]),
+    "gpurir_last_timing": (c_int, [c_void_p, fptr, fptr]),
+    "gpurir_last_transfer_bytes": (c_int, [c_void_p, u64ptr, u64ptr]),
+    "gpurir_probe_peaks": (c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 
 

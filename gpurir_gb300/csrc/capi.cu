@@ -23,12 +23,13 @@ int ism_forward_blocks_per_sm(int tpl, size_t smem);
 cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
-                               int em, int max_nsub, int grid, cudaStream_t st);
+                               int em, int max_nsub, int clamp, int grid, cudaStream_t st);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, int noise_kind, float *env_out, cudaStream_t st);
 cudaError_t philox_stream_launch(uint32_t *out, long n, uint64_t seed, uint64_t offset,
                                  uint32_t rir, cudaStream_t st);
+cudaError_t probe_peaks(double *fp32_flops, double *mufu_ops, cudaStream_t st);
 }  // namespace gpurir
 
 using namespace gpurir;
@@ -68,6 +69,10 @@ struct gpurir_sim {
     int *h_ctl = nullptr;      // pinned copy of the status word
     long last_n_rir = 0;
     size_t env_off = 0;        // offset of the envelope array in d_ws
+    int profile = 0;           // record events around each kernel
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ev_ism = false, ev_tail = false;
+    uint64_t last_h2d = 0, last_d2h = 0;
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -117,6 +122,8 @@ extern "C" int gpurir_destroy(gpurir_sim *s) {
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
     if (s->stage_done) cudaEventDestroy(s->stage_done);
     if (s->ws_busy) cudaEventDestroy(s->ws_busy);
+    for (int i = 0; i < 4; i++)
+        if (s->ev[i]) cudaEventDestroy(s->ev[i]);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return GPURIR_OK;
@@ -274,7 +281,7 @@ static int ensure_stage(gpurir_sim *s, size_t bytes) {
 }
 
 struct Plan {
-    int tpl, em, nsub, grid;
+    int tpl, em, nsub, grid, clamp;
     std::vector<IsmItem> items;
     std::vector<IsmItem> rirs;
 };
@@ -285,6 +292,10 @@ static int plan_single_room(gpurir_sim *s, const RoomDesc &R, int M_src, int M_r
     if (P.tpl < 0) return fail(GPURIR_ERR_UNSUPPORTED, "window too long (Fs above ~190 kHz)");
     const int sub = 32 * P.tpl;
     P.em = (int)align_up((size_t)std::ceil(R.H) + 2, 32);
+    {   // taps k in [floor(-H)+1, floor(H)]: without padding taps, |k - f| < H always holds
+        const int k_lo = (int)std::floor(-R.H) + 1, nk = (int)std::floor(R.H) - k_lo + 1;
+        P.clamp = (nk != sub || R.H != std::floor(R.H)) ? 1 : 0;
+    }
     const int max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
     if (max_nsub < 1) return fail(GPURIR_ERR_UNSUPPORTED, "window too long for shared memory");
     const long M = (long)M_src * M_rcv;
@@ -392,14 +403,21 @@ static int simulate_one_room(gpurir_sim *s, const float room_sz[3], const float 
     s->stage_pending = true;
     float *dout = host_io ? reinterpret_cast<float *>(d + o_out) : out;
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + o_room);
+    s->ev_ism = s->ev_tail = false;
+    s->last_h2d = stage_bytes;
+    s->last_d2h = sizeof(int) + (host_io ? (uint64_t)M * R.n_total * sizeof(float) : 0);
+    if (s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, s->d_ctl, s->d_ctl + 1,
-                              P.em, P.nsub, P.grid, st));
+                              P.em, P.nsub, P.clamp, P.grid, st));
+    if (s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
     const int n_diff = R.n_total - R.n_ism;
+    if (s->profile && n_diff > 0) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
     if (n_diff > 0)
         CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + o_rirs), (int)M, n_diff, dps, dpr,
                        dout, s->seed, s->calls, s->noise, reinterpret_cast<float *>(d + o_env), st));
+    if (s->ev_tail) CK(cudaEventRecord(s->ev[3], st));
     s->env_off = o_env;
     s->last_n_rir = n_diff > 0 ? M : 0;
     s->calls++;
@@ -433,7 +451,7 @@ extern "C" int gpurir_simulate_rir_device(gpurir_sim *s, const float room_sz[3],
                                           const int nb_img[3], float Tdiff, float Tmax, float Fs,
                                           float c, float *d_rir_out, void *stream) {
     if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
-    cudaStream_t st = stream ? reinterpret_cast<cudaStream_t>(stream) : s->stream;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);   // NULL: the CUDA default stream
     return simulate_one_room(s, room_sz, beta, d_pos_src, M_src, d_pos_rcv, d_orV_src, d_orV_rcv,
                              spkr_pattern, mic_pattern, M_rcv, nb_img, Tdiff, Tmax, Fs, c,
                              d_rir_out, false, st);
@@ -452,5 +470,40 @@ extern "C" int gpurir_last_envelope(gpurir_sim *s, float *out, long n) {
     if (n <= 0) return GPURIR_OK;
     if (s->ws_recorded) CK(cudaEventSynchronize(s->ws_busy));
     CK(cudaMemcpy(out, s->d_ws + s->env_off, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost));
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_probe_peaks(double *fp32_flops, double *mufu_ops) {
+    if (!fp32_flops || !mufu_ops) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    CK(probe_peaks(fp32_flops, mufu_ops, nullptr));
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_set_profiling(gpurir_sim *s, int on) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    if (on && !s->ev[0])
+        for (int i = 0; i < 4; i++) CK(cudaEventCreate(&s->ev[i]));
+    s->profile = on ? 1 : 0;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_last_timing(gpurir_sim *s, float *ism_ms, float *tail_ms) {
+    if (!s || !ism_ms || !tail_ms) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *ism_ms = *tail_ms = 0.0f;
+    if (s->ev_ism) {
+        CK(cudaEventSynchronize(s->ev[1]));
+        CK(cudaEventElapsedTime(ism_ms, s->ev[0], s->ev[1]));
+    }
+    if (s->ev_tail) {
+        CK(cudaEventSynchronize(s->ev[3]));
+        CK(cudaEventElapsedTime(tail_ms, s->ev[2], s->ev[3]));
+    }
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_last_transfer_bytes(gpurir_sim *s, uint64_t *h2d, uint64_t *d2h) {
+    if (!s || !h2d || !d2h) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *h2d = s->last_h2d;
+    *d2h = s->last_d2h;
     return GPURIR_OK;
 }

@@ -27,9 +27,10 @@ namespace gpurir {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 1024;                 // images per chunk
-constexpr int kRounds = kChunk / kThreads;   // 32-image rounds per warp and chunk
-constexpr int kMaxSub = 64;                  // sub-ranges per item
+constexpr int kChunk = 2048;                        // images per chunk
+constexpr int kPerWarp = kChunk / kWarps;           // images per warp and chunk
+constexpr int kRounds = kPerWarp / 32;              // 32-image rounds per warp and chunk
+constexpr int kMaxSub = 64;                         // sub-ranges per item
 
 struct IsmLaunch {
     const RoomDesc *rooms;
@@ -42,6 +43,7 @@ struct IsmLaunch {
     int *status;                      // device error word
     int em;                           // pad words before/after the buffers
     int max_nsub;                     // sub-ranges this launch's smem holds
+    int clamp;                        // taps may fall outside |x| < H: clamp the window
 };
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -50,19 +52,54 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
+// Taps of one image into its sub-range buffer: lane l owns taps
+// k = k_lo + l + 32 i, i < TPL, at p[32 i].
+template <int TPL, bool CLAMP>
+__device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], float al, float f,
+                                             float H2, float wc0, float wc1, float wc2, float wc3) {
+#pragma unroll
+    for (int i = 0; i < TPL; i++) {
+        const float x = kf[i] - f;
+        const float z = x * x;
+        float d = H2 - z;
+        if (CLAMP) d = fmaxf(d, 0.0f);
+        const float poly = fmaf(fmaf(fmaf(wc3, z, wc2), z, wc1), z, wc0);
+        const float cw = d * poly;                  // cos(pi x / Tw)
+        const float v = (cw * cw) * rcp_approx(x);  // Hann window / x
+        p[32 * i] = fmaf(al, v, p[32 * i]);
+    }
+}
+
+template <int TPL, bool CLAMP>
+__device__ __forceinline__ void scatter_list(float *bs, int origin, const float4 *rec,
+                                             const unsigned short *perm, int j0, int j1,
+                                             const float (&kf)[TPL], float lane_sign, float H2,
+                                             float wc0, float wc1, float wc2, float wc3) {
+    if (j0 >= j1) return;
+    float4 r = rec[perm[j0]];
+#pragma unroll 1
+    for (int j = j0; j < j1; j++) {
+        const float4 cur = r;
+        if (j + 1 < j1) r = rec[perm[j + 1]];   // fetch the next record while this one computes
+        scatter_taps<TPL, CLAMP>(bs + (__float_as_int(cur.z) - origin), kf, cur.x * lane_sign,
+                                 cur.y, H2, wc0, wc1, wc2, wc3);
+    }
+}
+
 template <int TPL>
 __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     constexpr int KS = 32 * TPL;   // taps per image, rounded up to the warp
-    constexpr int SUB = KS;        // sub-range length: keeps buffers of s, s+2 apart
+    constexpr int SUB = KS;        // sub-range length
     constexpr int BUF = SUB + KS;  // words per sub-range buffer
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *stage = reinterpret_cast<float4 *>(smem_raw);
-    float4 *sorted = stage + kChunk;
-    int *hist = reinterpret_cast<int *>(sorted + kChunk);   // [kWarps][kMaxSub]
+    float4 *rec = reinterpret_cast<float4 *>(smem_raw);                       // [kChunk]
+    unsigned short *perm = reinterpret_cast<unsigned short *>(rec + kChunk);  // [kChunk]
+    int *hist = reinterpret_cast<int *>(perm + kChunk);                        // [kWarps][kMaxSub]
     int *sub_start = hist + kWarps * kMaxSub;
     int *sub_cnt = sub_start + kMaxSub;
-    int *ctl = sub_cnt + kMaxSub;                             // [0] item, [1] queue
+    int *order = sub_cnt + kMaxSub;
+    int *ctl = order + kMaxSub;                                                // [0] item, [1] queue
     float *buf = reinterpret_cast<float *>(ctl + 4);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -116,15 +153,15 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 #pragma unroll
         for (int i = 0; i < TPL; i++) kf[i] = (float)(k_lo + lane + 32 * i);
         const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
+        int *my_hist = hist + warp * kMaxSub;
 
         for (int cbase = 0; cbase < n_img; cbase += kChunk) {
-            // ---- pass 1: geometry of this warp's 64 images, per-warp histogram
-            int *my_hist = hist + warp * kMaxSub;
+            // ---- pass 1: geometry of this warp's images, per-warp histogram
             for (int s = lane; s < nsub; s += 32) my_hist[s] = 0;
             __syncwarp();
 #pragma unroll 1
             for (int r = 0; r < kRounds; r++) {
-                const int local = warp * (32 * kRounds) + r * 32 + lane;
+                const int local = warp * kPerWarp + r * 32 + lane;
                 const int i = cbase + local;
                 int sub = -1;
                 float a = 0.f, f = 0.f;
@@ -172,83 +209,86 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                         sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
                     }
                 }
-                stage[local] = make_float4(a, f, __int_as_float(n0), __int_as_float(sub));
+                rec[local] = make_float4(a, f, __int_as_float(n0), __int_as_float(sub));
                 const unsigned peers = __match_any_sync(0xffffffffu, sub);
                 if (sub >= 0 && (peers & lt_mask) == 0) my_hist[sub] += __popc(peers);
                 __syncwarp();
             }
             __syncthreads();
-            // ---- scan: per-warp offsets, stable in image order
-            if (tid < nsub) {
-                int run = 0;
-                for (int w = 0; w < kWarps; w++) {
-                    int c = hist[w * kMaxSub + tid];
-                    hist[w * kMaxSub + tid] = run;
-                    run += c;
-                }
-                sub_cnt[tid] = run;
-            }
-            if (tid == 0) ctl[1] = 0;
-            __syncthreads();
+            // ---- warp 0: stable offsets per (warp, sub-range), starts, longest-first order
             if (warp == 0) {
-                int c0 = lane < nsub ? sub_cnt[lane] : 0;
-                int c1 = lane + 32 < nsub ? sub_cnt[lane + 32] : 0;
-                int x0 = c0, x1 = c1;
+                int cnt2[2], st2[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int s = lane + 32 * h;
+                    int run = 0;
+                    if (s < nsub)
+                        for (int w = 0; w < kWarps; w++) {
+                            const int c = hist[w * kMaxSub + s];
+                            hist[w * kMaxSub + s] = run;
+                            run += c;
+                        }
+                    cnt2[h] = run;
+                }
+                int x0 = cnt2[0], x1 = cnt2[1];
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    int y0 = __shfl_up_sync(0xffffffffu, x0, o);
-                    int y1 = __shfl_up_sync(0xffffffffu, x1, o);
+                    const int y0 = __shfl_up_sync(0xffffffffu, x0, o);
+                    const int y1 = __shfl_up_sync(0xffffffffu, x1, o);
                     if (lane >= o) { x0 += y0; x1 += y1; }
                 }
-                int tot0 = __shfl_sync(0xffffffffu, x0, 31);
-                if (lane < nsub) sub_start[lane] = x0 - c0;
-                if (lane + 32 < nsub) sub_start[lane + 32] = tot0 + x1 - c1;
+                const int tot0 = __shfl_sync(0xffffffffu, x0, 31);
+                st2[0] = x0 - cnt2[0];
+                st2[1] = tot0 + x1 - cnt2[1];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int s = lane + 32 * h;
+                    if (s < nsub) {
+                        sub_start[s] = st2[h];
+                        sub_cnt[s] = cnt2[h];
+                        for (int w = 0; w < kWarps; w++) hist[w * kMaxSub + s] += st2[h];
+                    }
+                }
+                // rank by (count desc, index asc): the queue hands out heavy sub-ranges first
+                int rk0 = 0, rk1 = 0;
+                for (int t = 0; t < 64; t++) {
+                    const int ct = __shfl_sync(0xffffffffu, cnt2[t >> 5], t & 31);
+                    if (t < nsub) {
+                        rk0 += (ct > cnt2[0]) || (ct == cnt2[0] && t < lane);
+                        rk1 += (ct > cnt2[1]) || (ct == cnt2[1] && t < lane + 32);
+                    }
+                }
+                if (lane < nsub) order[rk0] = lane;
+                if (lane + 32 < nsub) order[rk1] = lane + 32;
+                if (lane == 0) ctl[1] = 0;
             }
             __syncthreads();
-            for (int e = tid; e < kWarps * kMaxSub; e += kThreads) {
-                int s = e % kMaxSub;
-                if (s < nsub) hist[e] += sub_start[s];
-            }
-            __syncthreads();
-            // ---- pass 2: stable scatter into sub-range order
+            // ---- pass 2: stable permutation into sub-range order
 #pragma unroll 1
             for (int r = 0; r < kRounds; r++) {
-                const int local = warp * (32 * kRounds) + r * 32 + lane;
-                const float4 rec = stage[local];
-                const int sub = __float_as_int(rec.w);
+                const int local = warp * kPerWarp + r * 32 + lane;
+                const int sub = __float_as_int(rec[local].w);
                 const unsigned peers = __match_any_sync(0xffffffffu, sub);
-                if (sub >= 0) sorted[my_hist[sub] + __popc(peers & lt_mask)] = rec;
+                if (sub >= 0) perm[my_hist[sub] + __popc(peers & lt_mask)] = (unsigned short)local;
                 __syncwarp();
                 if (sub >= 0 && (peers & lt_mask) == 0) my_hist[sub] += __popc(peers);
                 __syncwarp();
             }
             __syncthreads();
-            // ---- pass 3: warps pull sub-ranges, scatter taps into private buffers
+            // ---- pass 3: warps pull sub-ranges (heaviest first), scatter taps into private buffers
             for (;;) {
-                int s = 0;
-                if (lane == 0) s = atomicAdd(&ctl[1], 1);
-                s = __shfl_sync(0xffffffffu, s, 0);
-                if (s >= nsub) break;
+                int q = 0;
+                if (lane == 0) q = atomicAdd(&ctl[1], 1);
+                q = __shfl_sync(0xffffffffu, q, 0);
+                if (q >= nsub) break;
+                const int s = order[q];
                 const int j0 = sub_start[s], j1 = j0 + sub_cnt[s];
                 float *bs = buf + P.em + s * BUF + lane;
                 const int origin = t_lo + s * SUB;
-#pragma unroll 1
-                for (int j = j0; j < j1; j++) {
-                    const float4 rec = sorted[j];
-                    const float al = rec.x * lane_sign;
-                    const float f = rec.y;
-                    float *p = bs + (__float_as_int(rec.z) - origin);
-#pragma unroll
-                    for (int i = 0; i < TPL; i++) {
-                        const float x = kf[i] - f;
-                        const float z = x * x;
-                        const float d = fmaxf(H2 - z, 0.0f);
-                        const float poly = fmaf(fmaf(fmaf(wc3, z, wc2), z, wc1), z, wc0);
-                        const float cw = d * poly;
-                        const float v = (cw * cw) * rcp_approx(x);
-                        p[32 * i] = fmaf(al, v, p[32 * i]);
-                    }
-                }
+                if (P.clamp)
+                    scatter_list<TPL, true>(bs, origin, rec, perm, j0, j1, kf, lane_sign, H2, wc0, wc1, wc2, wc3);
+                else
+                    scatter_list<TPL, false>(bs, origin, rec, perm, j0, j1, kf, lane_sign, H2, wc0, wc1, wc2, wc3);
             }
             __syncthreads();
         }
@@ -273,7 +313,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 // ---------------------------------------------------------------------------
 size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub) {
     const int ks = 32 * tpl;
-    size_t fixed = 2 * kChunk * sizeof(float4) + (kWarps * kMaxSub + 2 * kMaxSub + 4) * sizeof(int);
+    size_t fixed = kChunk * (sizeof(float4) + sizeof(unsigned short)) +
+                   (kWarps * kMaxSub + 3 * kMaxSub + 4) * sizeof(int);
     return fixed + (size_t)(2 * em + max_nsub * 2 * ks) * sizeof(float);
 }
 
@@ -323,12 +364,12 @@ int ism_forward_blocks_per_sm(int tpl, size_t smem) {
 cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
-                               int em, int max_nsub, int grid, cudaStream_t st) {
+                               int em, int max_nsub, int clamp, int grid, cudaStream_t st) {
     IsmLaunch p;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
     p.out = out; p.work_counter = work_counter; p.status = status;
-    p.em = em; p.max_nsub = max_nsub;
+    p.em = em; p.max_nsub = max_nsub; p.clamp = clamp;
     size_t smem = ism_forward_smem_bytes(tpl, em, max_nsub);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;

@@ -10,8 +10,9 @@
  * A handle owns one CUDA stream, a grow-only device workspace and pinned
  * staging memory.  A handle is not thread-safe: use one per host thread.
  * Functions with a `stream` argument are stream-ordered on that stream
- * (NULL means the handle's own stream) and return before the GPU finishes;
- * the others block until their results are on the host.
+ * (NULL is the CUDA default stream, as in the runtime API) and return before
+ * the GPU finishes; the others run on the handle's own stream and block until
+ * their results are on the host.
  *
  * Array layouts are C order; positions are [count][3] float32 metres.
  * Polar patterns: 0 omni, 1 homni, 2 card, 3 hypcard, 4 subcard, 5 bidir
@@ -107,6 +108,23 @@ int gpurir_philox_stream_device(uint64_t seed, uint64_t call_counter, uint32_t r
 /* Envelope of the last simulate call on this handle: per RIR (A, alpha, tau_dp)
  * as the tail used them (src/gpuRIR_cuda.cu:415-443).  `out` holds 3*n floats. */
 int gpurir_last_envelope(gpurir_sim *sim, float *out, long n);
+
+/* Kernel timing: when on, each simulate call records CUDA events on its
+ * stream around the ISM kernel and the tail kernel; gpurir_last_timing waits
+ * for them and returns the two durations in ms (0 for a kernel not launched).
+ * No counterpart in the reference. */
+int gpurir_set_profiling(gpurir_sim *sim, int on);
+int gpurir_last_timing(gpurir_sim *sim, float *ism_ms, float *tail_ms);
+
+/* Bytes the last simulate call copied host->device (descriptors, and for the
+ * host entry the positions) and device->host (status word, and for the host
+ * entry the RIRs).  No counterpart in the reference. */
+int gpurir_last_transfer_bytes(gpurir_sim *sim, uint64_t *h2d, uint64_t *d2h);
+
+/* Measured throughput of this device's FP32 FMA pipe (FLOP/s, 2 per FMA) and
+ * MUFU pipe (reciprocals/s): the peaks of the sinc-accumulation roofline.
+ * No counterpart in the reference (which has no roofline accounting). */
+int gpurir_probe_peaks(double *fp32_flops, double *mufu_ops);
 
 #ifdef __cplusplus
 }
