@@ -49,7 +49,8 @@ static int fail(int code, const std::string &msg) {
     } while (0)
 
 // Per-ISM-launch smem budget: two blocks of 512 threads per SM.
-static const size_t kSmemBudget = 110 * 1024;
+static const size_t kSmemBudget = 113 * 1024;   // two blocks per SM (228 KB less 1 KB each)
+static const size_t kSmemBudgetLarge = 220 * 1024;
 
 struct gpurir_sim {
     int mp = 0, lut = 0;
@@ -291,12 +292,14 @@ static int plan_single_room(gpurir_sim *s, const RoomDesc &R, int M_src, int M_r
     P.tpl = ism_forward_pick_tpl(R.H);
     if (P.tpl < 0) return fail(GPURIR_ERR_UNSUPPORTED, "window too long (Fs above ~190 kHz)");
     const int sub = 32 * P.tpl;
-    P.em = (int)align_up((size_t)std::ceil(R.H) + 2, 32);
+    P.em = (int)align_up((size_t)std::ceil(R.H) + 2, 4);
     {   // taps k in [floor(-H)+1, floor(H)]: without padding taps, |k - f| < H always holds
         const int k_lo = (int)std::floor(-R.H) + 1, nk = (int)std::floor(R.H) - k_lo + 1;
         P.clamp = (nk != sub || R.H != std::floor(R.H)) ? 1 : 0;
     }
-    const int max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
+    int max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
+    if (max_nsub < 4)   // long windows (high Fs): one block per SM with the whole shared memory
+        max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudgetLarge);
     if (max_nsub < 1) return fail(GPURIR_ERR_UNSUPPORTED, "window too long for shared memory");
     const long M = (long)M_src * M_rcv;
     const int n_ism = R.n_ism;
@@ -321,6 +324,7 @@ static int plan_single_room(gpurir_sim *s, const RoomDesc &R, int M_src, int M_r
     long n_seg = std::max(min_seg, std::min(want, cap));
     long tseg = align_up((size_t)((n_ism + n_seg - 1) / n_seg), 32);
     if (tseg > seg_max) tseg = seg_max;
+    if (tseg > 16384) tseg = 16384;   // image offsets are stored as int16 relative to t_lo
     n_seg = (n_ism + tseg - 1) / tseg;
     P.nsub = (int)((tseg + sub - 1) / sub);
     P.items.reserve(M * n_seg);

@@ -20,7 +20,8 @@
 // Tap value: amp * w(x) * sinc(x) with x = t - tau, written as
 //   a * (-1)^k * cos^2(pi x / Tw) / x,  a = -amp sin(pi f)/pi,  tau = n0 + f,
 // since sin(pi (k - f)) = -(-1)^k sin(pi f): one sinpi per image, one MUFU.RCP
-// per tap, and the Hann window as an FMA polynomial (image_sample, :116-121).
+// per tap, and the Hann window by the angle-sum identity from per-lane
+// constants and a per-image (cos, sin) pair (image_sample, :116-121).
 #include "gpurir_internal.cuh"
 
 namespace gpurir {
@@ -31,6 +32,8 @@ constexpr int kChunk = 2048;                        // images per chunk
 constexpr int kPerWarp = kChunk / kWarps;           // images per warp and chunk
 constexpr int kRounds = kPerWarp / 32;              // 32-image rounds per warp and chunk
 constexpr int kMaxSub = 64;                         // sub-ranges per item
+constexpr int kPool = kWarps;                       // extra slices of heavy sub-ranges per chunk
+constexpr int kMaxItems = 128;                      // >= kMaxSub + kPool queue entries
 
 struct IsmLaunch {
     const RoomDesc *rooms;
@@ -53,36 +56,43 @@ __device__ __forceinline__ float rcp_approx(float x) {
 }
 
 // Taps of one image into its sub-range buffer: lane l owns taps
-// k = k_lo + l + 32 i, i < TPL, at p[32 i].
+// k = k_lo + l + 32 i, i < TPL, at p[32 i].  With x = k - f the Hann window is
+//   0.5 (1 + cos(2 pi x / Tw)) = 0.5 + [0.5 cos(2 pi k/Tw)] cos(phi) + [0.5 sin(2 pi k/Tw)] sin(phi),
+// phi = 2 pi f / Tw: the bracketed factors are per-lane constants (ck, sk) and
+// (cos phi, sin phi) comes with the image, so a tap costs one FADD, two FFMA,
+// one MUFU.RCP, one FMUL and the shared-memory accumulate.
 template <int TPL, bool CLAMP>
-__device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], float al, float f,
-                                             float H2, float wc0, float wc1, float wc2, float wc3) {
+__device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], const float (&ck)[TPL],
+                                             const float (&sk)[TPL], float al, float4 r, float H) {
+    const float f = r.y, cphi = r.z, sphi = r.w;
 #pragma unroll
     for (int i = 0; i < TPL; i++) {
         const float x = kf[i] - f;
-        const float z = x * x;
-        float d = H2 - z;
-        if (CLAMP) d = fmaxf(d, 0.0f);
-        const float poly = fmaf(fmaf(fmaf(wc3, z, wc2), z, wc1), z, wc0);
-        const float cw = d * poly;                  // cos(pi x / Tw)
-        const float v = (cw * cw) * rcp_approx(x);  // Hann window / x
+        const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
+        float v = w * rcp_approx(x);
+        if (CLAMP) v = fabsf(x) < H ? v : 0.0f;
         p[32 * i] = fmaf(al, v, p[32 * i]);
     }
 }
 
 template <int TPL, bool CLAMP>
-__device__ __forceinline__ void scatter_list(float *bs, int origin, const float4 *rec,
+__device__ __forceinline__ void scatter_list(float *bs, int origin, const float4 *rec, const short *rec_n0,
                                              const unsigned short *perm, int j0, int j1,
-                                             const float (&kf)[TPL], float lane_sign, float H2,
-                                             float wc0, float wc1, float wc2, float wc3) {
-    if (j0 >= j1) return;
-    float4 r = rec[perm[j0]];
+                                             const float (&kf)[TPL], const float (&ck)[TPL],
+                                             const float (&sk)[TPL], float lane_sign, float H) {
+    int j = j0;
 #pragma unroll 1
-    for (int j = j0; j < j1; j++) {
-        const float4 cur = r;
-        if (j + 1 < j1) r = rec[perm[j + 1]];   // fetch the next record while this one computes
-        scatter_taps<TPL, CLAMP>(bs + (__float_as_int(cur.z) - origin), kf, cur.x * lane_sign,
-                                 cur.y, H2, wc0, wc1, wc2, wc3);
+    for (; j + 1 < j1; j += 2) {   // two images per trip: half the loop bookkeeping
+        const int ia = perm[j], ib = perm[j + 1];
+        const float4 a = rec[ia], b = rec[ib];
+        const int na = rec_n0[ia], nb = rec_n0[ib];
+        scatter_taps<TPL, CLAMP>(bs + (na - origin), kf, ck, sk, a.x * lane_sign, a, H);
+        scatter_taps<TPL, CLAMP>(bs + (nb - origin), kf, ck, sk, b.x * lane_sign, b, H);
+    }
+    if (j < j1) {
+        const int ia = perm[j];
+        const float4 a = rec[ia];
+        scatter_taps<TPL, CLAMP>(bs + (rec_n0[ia] - origin), kf, ck, sk, a.x * lane_sign, a, H);
     }
 }
 
@@ -93,15 +103,18 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     constexpr int BUF = SUB + KS;  // words per sub-range buffer
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *rec = reinterpret_cast<float4 *>(smem_raw);                       // [kChunk]
-    unsigned short *perm = reinterpret_cast<unsigned short *>(rec + kChunk);  // [kChunk]
-    int *hist = reinterpret_cast<int *>(perm + kChunk);                        // [kWarps][kMaxSub]
+    float4 *rec = reinterpret_cast<float4 *>(smem_raw);            // [kChunk] a, f, cos phi, sin phi
+    short *rec_n0 = reinterpret_cast<short *>(rec + kChunk);        // [kChunk] floor(tau) - t_lo
+    unsigned short *perm = reinterpret_cast<unsigned short *>(rec_n0 + kChunk);  // [kChunk]
+    signed char *rec_sub = reinterpret_cast<signed char *>(perm + kChunk);       // [kChunk]
+    int *hist = reinterpret_cast<int *>(rec_sub + kChunk);          // [kWarps][kMaxSub]
     int *sub_start = hist + kWarps * kMaxSub;
     int *sub_cnt = sub_start + kMaxSub;
-    int *order = sub_cnt + kMaxSub;
-    int *ctl = order + kMaxSub;                                                // [0] item, [1] queue
-    float *buf = reinterpret_cast<float *>(ctl + 4);
-
+    int *pool_base = sub_cnt + kMaxSub;                                        // first pool slot of s
+    int *order = pool_base + kMaxSub;                                          // [kMaxItems] s | k << 8
+    int *slot_sub = order + kMaxItems;                                         // [kPool]
+    int *ctl = slot_sub + kPool;   // [0] item, [1] queue, [2] queue length, [3] pool slots, [4] cap
+    float *buf = reinterpret_cast<float *>(ctl + 8);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
 
@@ -120,14 +133,16 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             continue;
         }
         const int buf_words = 2 * P.em + nsub * BUF;
-        for (int i = tid; i < buf_words; i += kThreads) buf[i] = 0.0f;
+        const int slot_words = 2 * P.em + BUF;
+        float *pool = buf + buf_words;   // kPool slots of [em | BUF | em]
+        for (int i = tid; i < buf_words + kPool * slot_words; i += kThreads) buf[i] = 0.0f;
 
         // Room and pair constants (uniform across the block).
         const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
         const int N0 = R.nb[0], N1 = R.nb[1], N2 = R.nb[2];
         const int n_img = R.n_img;
-        const float H = R.H, H2 = R.H2;
-        const float wc0 = R.wc[0], wc1 = R.wc[1], wc2 = R.wc[2], wc3 = R.wc[3];
+        const float H = R.H;
+        const float inv_h = 1.0f / H;
         const int k_lo = (int)floorf(-H) + 1;
         const int spkr = R.spkr, mic = R.mic;
         const ff kfs = {R.kh, R.kl};
@@ -149,9 +164,15 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const float keep_lo = (float)t_lo - H, keep_hi = (float)t_hi + H;
 
         // Per-lane tap constants: k = k_lo + lane + 32 i, sign (-1)^k.
-        float kf[TPL];
+        float kf[TPL], ck[TPL], sk[TPL];
 #pragma unroll
-        for (int i = 0; i < TPL; i++) kf[i] = (float)(k_lo + lane + 32 * i);
+        for (int i = 0; i < TPL; i++) {
+            kf[i] = (float)(k_lo + lane + 32 * i);
+            float sn, cs;
+            sincospif(kf[i] * inv_h, &sn, &cs);   // 2 pi k / Tw = pi k / H
+            ck[i] = 0.5f * cs;
+            sk[i] = 0.5f * sn;
+        }
         const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
         int *my_hist = hist + warp * kMaxSub;
 
@@ -164,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 const int local = warp * kPerWarp + r * 32 + lane;
                 const int i = cbase + local;
                 int sub = -1;
-                float a = 0.f, f = 0.f;
+                float a = 0.f, f = 0.f, sphi = 0.f, cphi = 1.f;
                 int n0 = 0;
                 if (i < n_img) {
                     const int q = i / N2;
@@ -204,18 +225,22 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
                     f = fmaxf(f, 9.094947017729282e-13f);   // 2^-40: keeps x = k - f != 0
                     a = -amp * sinpif(f) * 0.318309886183790672f;
+                    sincospif(f * inv_h, &sphi, &cphi);   // phi = 2 pi f / Tw
                     if (amp != 0.0f && tau.hi > keep_lo && tau.hi < keep_hi) {
                         int rel = n0 - t_lo;
                         sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
                     }
                 }
-                rec[local] = make_float4(a, f, __int_as_float(n0), __int_as_float(sub));
+                rec[local] = make_float4(a, f, cphi, sphi);
+                rec_n0[local] = (short)(sub >= 0 ? n0 - t_lo : 0);   // |.| < 2^15: host caps segments
+                rec_sub[local] = (signed char)sub;
                 const unsigned peers = __match_any_sync(0xffffffffu, sub);
                 if (sub >= 0 && (peers & lt_mask) == 0) my_hist[sub] += __popc(peers);
                 __syncwarp();
             }
             __syncthreads();
-            // ---- warp 0: stable offsets per (warp, sub-range), starts, longest-first order
+            // ---- warp 0: stable offsets per (warp, sub-range); split sub-ranges heavier than a
+            //      warp's share into slices; queue full slices first, then the rest by size
             if (warp == 0) {
                 int cnt2[2], st2[2];
 #pragma unroll
@@ -238,36 +263,70 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     if (lane >= o) { x0 += y0; x1 += y1; }
                 }
                 const int tot0 = __shfl_sync(0xffffffffu, x0, 31);
+                const int total = tot0 + __shfl_sync(0xffffffffu, x1, 31);
                 st2[0] = x0 - cnt2[0];
                 st2[1] = tot0 + x1 - cnt2[1];
+                const int cap = max(1, (total + kWarps - 1) / kWarps);
+                int full2[2], rem2[2], ext2[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    full2[h] = cnt2[h] / cap;
+                    rem2[h] = cnt2[h] - full2[h] * cap;
+                    ext2[h] = max(full2[h] + (rem2[h] > 0) - 1, 0);   // slices beyond the first
+                }
+                // exclusive scans of full slices and extra slices over s = 0..63
+                int f0 = full2[0], f1 = full2[1], e0 = ext2[0], e1 = ext2[1];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int a0 = __shfl_up_sync(0xffffffffu, f0, o), a1 = __shfl_up_sync(0xffffffffu, f1, o);
+                    const int b0 = __shfl_up_sync(0xffffffffu, e0, o), b1 = __shfl_up_sync(0xffffffffu, e1, o);
+                    if (lane >= o) { f0 += a0; f1 += a1; e0 += b0; e1 += b1; }
+                }
+                const int ftot0 = __shfl_sync(0xffffffffu, f0, 31), etot0 = __shfl_sync(0xffffffffu, e0, 31);
+                const int n_full = ftot0 + __shfl_sync(0xffffffffu, f1, 31);
+                const int n_extra = etot0 + __shfl_sync(0xffffffffu, e1, 31);
+                const int fpre[2] = {f0 - full2[0], ftot0 + f1 - full2[1]};
+                const int epre[2] = {e0 - ext2[0], etot0 + e1 - ext2[1]};
+                // remainder slices ranked by (size desc, s asc)
+                int rk[2] = {0, 0};
+                for (int t = 0; t < 64; t++) {
+                    const int rt = __shfl_sync(0xffffffffu, t < 32 ? rem2[0] : rem2[1], t & 31);
+                    if (t < nsub && rt > 0) {
+                        rk[0] += (rt > rem2[0]) || (rt == rem2[0] && t < lane);
+                        rk[1] += (rt > rem2[1]) || (rt == rem2[1] && t < lane + 32);
+                    }
+                }
+                int n_rem = 0;
+                for (int t = 0; t < 64; t++) {
+                    const int rt = __shfl_sync(0xffffffffu, t < 32 ? rem2[0] : rem2[1], t & 31);
+                    n_rem += (t < nsub && rt > 0);
+                }
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int s = lane + 32 * h;
                     if (s < nsub) {
                         sub_start[s] = st2[h];
                         sub_cnt[s] = cnt2[h];
+                        pool_base[s] = epre[h];
                         for (int w = 0; w < kWarps; w++) hist[w * kMaxSub + s] += st2[h];
+                        for (int k = 0; k < full2[h]; k++) order[fpre[h] + k] = s | (k << 8);
+                        if (rem2[h] > 0) order[n_full + rk[h]] = s | (full2[h] << 8);
+                        for (int k = 0; k < ext2[h]; k++) slot_sub[epre[h] + k] = s;
                     }
                 }
-                // rank by (count desc, index asc): the queue hands out heavy sub-ranges first
-                int rk0 = 0, rk1 = 0;
-                for (int t = 0; t < 64; t++) {
-                    const int ct = __shfl_sync(0xffffffffu, cnt2[t >> 5], t & 31);
-                    if (t < nsub) {
-                        rk0 += (ct > cnt2[0]) || (ct == cnt2[0] && t < lane);
-                        rk1 += (ct > cnt2[1]) || (ct == cnt2[1] && t < lane + 32);
-                    }
+                if (lane == 0) {
+                    ctl[1] = 0;
+                    ctl[2] = n_full + n_rem;
+                    ctl[3] = n_extra;
+                    ctl[4] = cap;
                 }
-                if (lane < nsub) order[rk0] = lane;
-                if (lane + 32 < nsub) order[rk1] = lane + 32;
-                if (lane == 0) ctl[1] = 0;
             }
             __syncthreads();
             // ---- pass 2: stable permutation into sub-range order
 #pragma unroll 1
             for (int r = 0; r < kRounds; r++) {
                 const int local = warp * kPerWarp + r * 32 + lane;
-                const int sub = __float_as_int(rec[local].w);
+                const int sub = rec_sub[local];
                 const unsigned peers = __match_any_sync(0xffffffffu, sub);
                 if (sub >= 0) perm[my_hist[sub] + __popc(peers & lt_mask)] = (unsigned short)local;
                 __syncwarp();
@@ -275,20 +334,37 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 __syncwarp();
             }
             __syncthreads();
-            // ---- pass 3: warps pull sub-ranges (heaviest first), scatter taps into private buffers
-            for (;;) {
-                int q = 0;
-                if (lane == 0) q = atomicAdd(&ctl[1], 1);
-                q = __shfl_sync(0xffffffffu, q, 0);
-                if (q >= nsub) break;
-                const int s = order[q];
-                const int j0 = sub_start[s], j1 = j0 + sub_cnt[s];
-                float *bs = buf + P.em + s * BUF + lane;
-                const int origin = t_lo + s * SUB;
-                if (P.clamp)
-                    scatter_list<TPL, true>(bs, origin, rec, perm, j0, j1, kf, lane_sign, H2, wc0, wc1, wc2, wc3);
-                else
-                    scatter_list<TPL, false>(bs, origin, rec, perm, j0, j1, kf, lane_sign, H2, wc0, wc1, wc2, wc3);
+            // ---- pass 3: warps pull slices, scatter taps into private buffers
+            {
+                const int n_q = ctl[2], cap = ctl[4];
+                for (;;) {
+                    int q = 0;
+                    if (lane == 0) q = atomicAdd(&ctl[1], 1);
+                    q = __shfl_sync(0xffffffffu, q, 0);
+                    if (q >= n_q) break;
+                    const int item = order[q];
+                    const int s = item & 255, k = item >> 8;
+                    const int j0 = sub_start[s] + k * cap;
+                    const int j1 = min(j0 + cap, sub_start[s] + sub_cnt[s]);
+                    float *bs = (k == 0 ? buf + s * BUF : pool + (pool_base[s] + k - 1) * slot_words) +
+                                P.em + lane;
+                    const int origin = s * SUB;   // record n0 is relative to t_lo
+                    if (P.clamp)
+                        scatter_list<TPL, true>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, lane_sign, H);
+                    else
+                        scatter_list<TPL, false>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, lane_sign, H);
+                }
+            }
+            __syncthreads();
+            // ---- merge the extra slices into their sub-range, in slice order (deterministic)
+            {
+                const int n_extra = ctl[3];
+                for (int w = tid; w < BUF; w += kThreads)
+                    for (int slot = 0; slot < n_extra; slot++) {
+                        float *src = pool + slot * slot_words + P.em + w;
+                        buf[P.em + slot_sub[slot] * BUF + w] += *src;
+                        *src = 0.0f;
+                    }
             }
             __syncthreads();
         }
@@ -313,8 +389,9 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 // ---------------------------------------------------------------------------
 size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub) {
     const int ks = 32 * tpl;
-    size_t fixed = kChunk * (sizeof(float4) + sizeof(unsigned short)) +
-                   (kWarps * kMaxSub + 3 * kMaxSub + 4) * sizeof(int);
+    size_t fixed = kChunk * (sizeof(float4) + sizeof(short) + sizeof(unsigned short) + 1) +
+                   (kWarps * kMaxSub + 3 * kMaxSub + kMaxItems + kPool + 8) * sizeof(int) +
+                   (size_t)kPool * (2 * em + 2 * ks) * sizeof(float);
     return fixed + (size_t)(2 * em + max_nsub * 2 * ks) * sizeof(float);
 }
 
@@ -341,7 +418,7 @@ static cudaError_t launch_tpl(const IsmLaunch &p, int grid, size_t smem, cudaStr
     static bool attr_set = false;   // per process; the attribute is per function
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(ism_forward_kernel<TPL>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
@@ -352,7 +429,7 @@ static cudaError_t launch_tpl(const IsmLaunch &p, int grid, size_t smem, cudaStr
 int ism_forward_blocks_per_sm(int tpl, size_t smem) {
     int n = 0;
     switch (tpl) {
-#define OCC(T) case T: cudaFuncSetAttribute(ism_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); \
+#define OCC(T) case T: cudaFuncSetAttribute(ism_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ism_forward_kernel<T>, kThreads, smem); break;
         OCC(2) OCC(4) OCC(8) OCC(12) OCC(16) OCC(24)
 #undef OCC
