@@ -49,6 +49,30 @@ SIGNATURES = {
 }
 
 
+class Room(ctypes.Structure):
+    """gpurir_room of include/gpurir_gb300.h."""
+    _fields_ = [("room_sz", ctypes.c_float * 3), ("beta", ctypes.c_float * 6),
+                ("nb_img", ctypes.c_int * 3), ("Tdiff", ctypes.c_float), ("Tmax", ctypes.c_float),
+                ("n_src", ctypes.c_int), ("n_rcv", ctypes.c_int), ("spkr_pattern", ctypes.c_int),
+                ("mic_pattern", ctypes.c_int)]
+
+
+llptr = ctypes.POINTER(ctypes.c_longlong)
+SIGNATURES.update({
+    "gpurir_batch_layout": (c_int, [c_int, ctypes.POINTER(Room), c_float, llptr]),
+    "gpurir_simulate_batch_device": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float,
+                                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                             c_void_p]),
+    "gpurir_batch_create": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float,
+                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    ctypes.POINTER(c_void_p)]),
+    "gpurir_batch_launch": (c_int, [c_void_p, c_void_p]),
+    "gpurir_batch_info": (c_int, [c_void_p, llptr, llptr]),
+    "gpurir_batch_destroy": (c_int, [c_void_p]),
+    "gpurir_device_status": (c_int, [c_void_p]),
+})
+
+
 class GpuRirError(RuntimeError):
     """A gpurir_gb300 C-ABI call returned a non-zero status."""
 

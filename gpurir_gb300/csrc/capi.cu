@@ -6,6 +6,7 @@
 // on any error.  Here a handle keeps a grow-only device workspace and pinned
 // staging memory, all launch descriptors go to the device in one copy, the
 // two kernels run back to back on one stream, and errors come back as codes.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,7 +27,8 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
-                        uint64_t offset, int noise_kind, float *env_out, cudaStream_t st);
+                        uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
+                        cudaStream_t st);
 cudaError_t philox_stream_launch(uint32_t *out, long n, uint64_t seed, uint64_t offset,
                                  uint32_t rir, cudaStream_t st);
 cudaError_t probe_peaks(double *fp32_flops, double *mufu_ops, cudaStream_t st);
@@ -283,58 +285,91 @@ static int ensure_stage(gpurir_sim *s, size_t bytes) {
 
 struct Plan {
     int tpl, em, nsub, grid, clamp;
+    int max_n_diff;
     std::vector<IsmItem> items;
     std::vector<IsmItem> rirs;
 };
 
-// Split every RIR of one room into segments and order the work.
-static int plan_single_room(gpurir_sim *s, const RoomDesc &R, int M_src, int M_rcv, Plan &P) {
-    P.tpl = ism_forward_pick_tpl(R.H);
+// Launch geometry shared by every room of a launch (all rooms use one Fs).
+static int plan_window(float H, Plan &P, int &max_nsub) {
+    P.tpl = ism_forward_pick_tpl(H);
     if (P.tpl < 0) return fail(GPURIR_ERR_UNSUPPORTED, "window too long (Fs above ~190 kHz)");
     const int sub = 32 * P.tpl;
-    P.em = (int)align_up((size_t)std::ceil(R.H) + 2, 4);
+    P.em = (int)align_up((size_t)std::ceil(H) + 2, 4);
     {   // taps k in [floor(-H)+1, floor(H)]: without padding taps, |k - f| < H always holds
-        const int k_lo = (int)std::floor(-R.H) + 1, nk = (int)std::floor(R.H) - k_lo + 1;
-        P.clamp = (nk != sub || R.H != std::floor(R.H)) ? 1 : 0;
+        const int k_lo = (int)std::floor(-H) + 1, nk = (int)std::floor(H) - k_lo + 1;
+        P.clamp = (nk != sub || H != std::floor(H)) ? 1 : 0;
     }
-    int max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
+    max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
     if (max_nsub < 4)   // long windows (high Fs): one block per SM with the whole shared memory
         max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudgetLarge);
     if (max_nsub < 1) return fail(GPURIR_ERR_UNSUPPORTED, "window too long for shared memory");
-    const long M = (long)M_src * M_rcv;
-    const int n_ism = R.n_ism;
+    return GPURIR_OK;
+}
+
+// Work items for a set of rooms.  Every RIR is cut into segments of at most
+// what one block's shared memory holds; RIRs of small launches are cut finer so
+// that the persistent grid has work for every SM.  Items are ordered by an
+// estimate of their cost, largest first (longest-processing-time order).
+static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
+    int max_nsub = 0;
+    int rc = plan_window(R[0].H, P, max_nsub);
+    if (rc) return rc;
+    const int sub = 32 * P.tpl;
+    long M_tot = 0;
+    P.max_n_diff = 0;
+    for (const RoomDesc &r : R) {
+        M_tot += (long)r.n_src * r.n_rcv;
+        P.max_n_diff = std::max(P.max_n_diff, r.n_total - r.n_ism);
+    }
     P.items.clear();
     P.rirs.clear();
-    P.rirs.reserve(M);
-    for (long m = 0; m < M; m++) {
-        IsmItem r{};
-        r.room = 0; r.src = (int)(m / M_rcv); r.rcv = (int)(m % M_rcv);
-        r.rir = (int)m;
-        r.out_row = (long long)m * R.n_total;
-        P.rirs.push_back(r);
-    }
+    P.rirs.reserve(M_tot);
+    const long seg_max = std::min<long>((long)max_nsub * sub, 16384);   // int16 image offsets
+    const long target = 4L * s->num_sms;
+    const long want = (target + M_tot - 1) / std::max<long>(M_tot, 1);
+    std::vector<std::pair<double, IsmItem>> work;
     P.nsub = 1;
-    P.grid = 0;
-    if (n_ism <= 0) return GPURIR_OK;
-    const long seg_max = (long)max_nsub * sub;
-    long min_seg = (n_ism + seg_max - 1) / seg_max;
-    long target = 4L * s->num_sms;
-    long want = (target + M - 1) / M;
-    long cap = (n_ism + sub - 1) / sub;
-    long n_seg = std::max(min_seg, std::min(want, cap));
-    long tseg = align_up((size_t)((n_ism + n_seg - 1) / n_seg), 32);
-    if (tseg > seg_max) tseg = seg_max;
-    if (tseg > 16384) tseg = 16384;   // image offsets are stored as int16 relative to t_lo
-    n_seg = (n_ism + tseg - 1) / tseg;
-    P.nsub = (int)((tseg + sub - 1) / sub);
-    P.items.reserve(M * n_seg);
-    for (long g = n_seg - 1; g >= 0; g--)   // later segments hold more images: start them first
-        for (long m = 0; m < M; m++) {
-            IsmItem it = P.rirs[m];
-            it.t_lo = (int)(g * tseg);
-            it.t_hi = (int)std::min<long>((g + 1) * tseg, n_ism);
-            P.items.push_back(it);
+    for (size_t ri = 0; ri < R.size(); ri++) {
+        const RoomDesc &r = R[ri];
+        const long M = (long)r.n_src * r.n_rcv;
+        long n_seg = 0, tseg = 0;
+        if (r.n_ism > 0) {
+            const long min_seg = (r.n_ism + seg_max - 1) / seg_max;
+            const long cap = (r.n_ism + sub - 1) / sub;
+            n_seg = std::max(min_seg, std::min(want, cap));
+            tseg = std::min<long>(align_up((size_t)((r.n_ism + n_seg - 1) / n_seg), 32), seg_max);
+            n_seg = (r.n_ism + tseg - 1) / tseg;
+            P.nsub = std::max<int>(P.nsub, (int)((tseg + sub - 1) / sub));
         }
+        for (long m = 0; m < M; m++) {
+            IsmItem it{};
+            it.room = (int)ri;
+            it.src = r.src_off + (int)(m / r.n_rcv);
+            it.rcv = r.rcv_off + (int)(m % r.n_rcv);
+            it.rir = r.rir_off + (int)m;
+            it.out_row = r.out_off + (long long)m * r.n_total;
+            P.rirs.push_back(it);
+            for (long g = 0; g < n_seg; g++) {
+                IsmItem w = it;
+                w.t_lo = (int)(g * tseg);
+                w.t_hi = (int)std::min<long>((g + 1) * tseg, r.n_ism);
+                // images in the segment's delay range (density grows with delay^2), plus
+                // the geometry pass over every image of the room
+                const double a = (double)w.t_lo / r.n_ism, b = (double)w.t_hi / r.n_ism;
+                const double cost = r.n_img * ((b * b * b - a * a * a) + 0.15);
+                work.push_back({cost, w});
+            }
+        }
+    }
+    std::stable_sort(work.begin(), work.end(),
+                     [](const std::pair<double, IsmItem> &x, const std::pair<double, IsmItem> &y) {
+                         return x.first > y.first;
+                     });
+    P.items.reserve(work.size());
+    for (auto &w : work) P.items.push_back(w.second);
+    P.grid = 0;
+    if (P.items.empty()) return GPURIR_OK;
     size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub);
     int bps = ism_forward_blocks_per_sm(P.tpl, smem);
     if (bps < 1) return fail(GPURIR_ERR_CUDA, "ISM kernel does not fit on an SM");
@@ -351,7 +386,106 @@ static int check_status(gpurir_sim *s) {
     return GPURIR_OK;
 }
 
-// Shared body of the host and device entry points.
+// Byte layout of one launch's descriptors (mirrored host staging -> device).
+struct Layout {
+    size_t o_rooms, o_items, o_rirs, o_pos, stage_bytes, o_env, o_out, dev_bytes;
+};
+
+static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv, long M,
+                          long long out_elems, bool host_io) {
+    Layout L;
+    L.o_rooms = 0;
+    L.o_items = align_up(L.o_rooms + n_rooms * sizeof(RoomDesc), 256);
+    L.o_rirs = align_up(L.o_items + P.items.size() * sizeof(IsmItem), 256);
+    L.o_pos = align_up(L.o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
+    size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
+    L.stage_bytes = align_up(L.o_pos + n_pos * sizeof(float), 256);
+    L.o_env = L.stage_bytes;
+    L.o_out = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
+    L.dev_bytes = L.o_out + (host_io ? (size_t)out_elems * sizeof(float) : 0);
+    return L;
+}
+
+static void fill_stage(char *h, const Layout &L, const std::vector<RoomDesc> &R, const Plan &P) {
+    memcpy(h + L.o_rooms, R.data(), R.size() * sizeof(RoomDesc));
+    if (!P.items.empty()) memcpy(h + L.o_items, P.items.data(), P.items.size() * sizeof(IsmItem));
+    if (!P.rirs.empty()) memcpy(h + L.o_rirs, P.rirs.data(), P.rirs.size() * sizeof(IsmItem));
+}
+
+// Enqueue the ISM and tail kernels of one planned launch on `st`.
+static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const Layout &L, long M,
+                           const float *dps, const float *dpr, const float *dos, const float *dor,
+                           float *dout, int *work_counter, const uint64_t *offset_ptr,
+                           cudaStream_t st, bool record) {
+    const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + L.o_rooms);
+    if (record && s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
+    if (P.grid > 0)
+        CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
+                              (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
+                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st));
+    if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
+    if (record && s->profile && P.max_n_diff > 0) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
+    if (P.max_n_diff > 0)
+        CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_rirs), (int)M, P.max_n_diff,
+                       dps, dpr, dout, s->seed, s->calls, offset_ptr, s->noise,
+                       reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env), st));
+    if (record && s->ev_tail) CK(cudaEventRecord(s->ev[3], st));
+    return GPURIR_OK;
+}
+
+// Shared body of the single-room and batched entry points, host or device I/O.
+// Rooms carry their source/receiver/RIR/output offsets already.
+static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, long n_rcv,
+                          const float *pos_src, const float *pos_rcv, const float *orV_src,
+                          const float *orV_rcv, float *out, long long out_elems, bool host_io,
+                          cudaStream_t st) {
+    Plan P;
+    int rc = plan_rooms(s, R, P);
+    if (rc) return rc;
+    const long M = (long)P.rirs.size();
+    Layout L = make_layout(P, R.size(), n_src, n_rcv, M, out_elems, host_io);
+    if ((rc = ensure_device(s, L.dev_bytes))) return rc;
+    if ((rc = ensure_stage(s, L.stage_bytes))) return rc;
+    char *h = s->h_stage;
+    fill_stage(h, L, R, P);
+    const float *dps = pos_src, *dpr = pos_rcv, *dos = orV_src, *dor = orV_rcv;
+    char *d = s->d_ws;
+    if (host_io) {
+        float *hp = reinterpret_cast<float *>(h + L.o_pos);
+        memcpy(hp, pos_src, sizeof(float) * 3 * n_src);
+        memcpy(hp + 3 * n_src, pos_rcv, sizeof(float) * 3 * n_rcv);
+        if (orV_src) memcpy(hp + 3 * (n_src + n_rcv), orV_src, sizeof(float) * 3 * n_src);
+        else memset(hp + 3 * (n_src + n_rcv), 0, sizeof(float) * 3 * n_src);
+        if (orV_rcv) memcpy(hp + 3 * (2 * n_src + n_rcv), orV_rcv, sizeof(float) * 3 * n_rcv);
+        else memset(hp + 3 * (2 * n_src + n_rcv), 0, sizeof(float) * 3 * n_rcv);
+        float *dp = reinterpret_cast<float *>(d + L.o_pos);
+        dps = dp; dpr = dp + 3 * n_src; dos = dp + 3 * (n_src + n_rcv); dor = dp + 3 * (2 * n_src + n_rcv);
+    }
+    if (s->ws_recorded) CK(cudaStreamWaitEvent(st, s->ws_busy, 0));   // earlier calls, any stream
+    CK(cudaMemcpyAsync(d, h, L.stage_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(s->stage_done, st));
+    s->stage_pending = true;
+    float *dout = host_io ? reinterpret_cast<float *>(d + L.o_out) : out;
+    s->ev_ism = s->ev_tail = false;
+    s->last_h2d = L.stage_bytes;
+    s->last_d2h = sizeof(int) + (host_io ? (uint64_t)out_elems * sizeof(float) : 0);
+    if ((rc = enqueue_kernels(s, P, d, L, M, dps, dpr, dos, dor, dout, s->d_ctl, nullptr, st, true)))
+        return rc;
+    s->env_off = L.o_env;
+    s->last_n_rir = P.max_n_diff > 0 ? M : 0;
+    s->calls++;
+    CK(cudaMemcpyAsync(s->h_ctl + 1, s->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (host_io)
+        CK(cudaMemcpyAsync(out, dout, (size_t)out_elems * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(s->ws_busy, st));
+    s->ws_recorded = true;
+    if (host_io) {
+        CK(cudaStreamSynchronize(st));
+        return check_status(s);
+    }
+    return GPURIR_OK;
+}
+
 static int simulate_one_room(gpurir_sim *s, const float room_sz[3], const float beta[6],
                              const float *pos_src, int M_src, const float *pos_rcv,
                              const float *orV_src, const float *orV_rcv, int spkr, int mic,
@@ -364,75 +498,41 @@ static int simulate_one_room(gpurir_sim *s, const float room_sz[3], const float 
     if ((spkr != 0 && !orV_src) || (mic != 0 && !orV_rcv))
         return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
     if ((long long)M_src * M_rcv > (1LL << 30)) return fail(GPURIR_ERR_INVALID, "too many RIRs");
-    RoomDesc R;
-    int rc = build_room(R, room_sz, beta, nb_img, Tdiff, Tmax, Fs, c, spkr, mic);
+    std::vector<RoomDesc> R(1);
+    int rc = build_room(R[0], room_sz, beta, nb_img, Tdiff, Tmax, Fs, c, spkr, mic);
     if (rc) return rc;
-    R.n_src = M_src; R.n_rcv = M_rcv;
-    Plan P;
-    rc = plan_single_room(s, R, M_src, M_rcv, P);
-    if (rc) return rc;
-    const long M = (long)M_src * M_rcv;
-    // Staging layout, mirrored byte for byte in the device workspace.
-    size_t o_room = 0;
-    size_t o_items = align_up(o_room + sizeof(RoomDesc), 256);
-    size_t o_rirs = align_up(o_items + P.items.size() * sizeof(IsmItem), 256);
-    size_t o_pos = align_up(o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
-    size_t n_pos = host_io ? (size_t)(M_src + M_rcv) * 3 * 2 : 0;
-    size_t stage_bytes = align_up(o_pos + n_pos * sizeof(float), 256);
-    size_t o_env = stage_bytes;
-    size_t o_out = align_up(o_env + (size_t)M * 3 * sizeof(float), 256);
-    size_t dev_bytes = o_out + (host_io ? (size_t)M * R.n_total * sizeof(float) : 0);
-    if ((rc = ensure_device(s, dev_bytes))) return rc;
-    if ((rc = ensure_stage(s, stage_bytes))) return rc;
-    char *h = s->h_stage;
-    memcpy(h + o_room, &R, sizeof(R));
-    if (!P.items.empty()) memcpy(h + o_items, P.items.data(), P.items.size() * sizeof(IsmItem));
-    memcpy(h + o_rirs, P.rirs.data(), P.rirs.size() * sizeof(IsmItem));
-    const float *dps = pos_src, *dpr = pos_rcv, *dos = orV_src, *dor = orV_rcv;
-    char *d = s->d_ws;
-    if (host_io) {
-        float *hp = reinterpret_cast<float *>(h + o_pos);
-        memcpy(hp, pos_src, sizeof(float) * 3 * M_src);
-        memcpy(hp + 3 * M_src, pos_rcv, sizeof(float) * 3 * M_rcv);
-        if (orV_src) memcpy(hp + 3 * (M_src + M_rcv), orV_src, sizeof(float) * 3 * M_src);
-        else memset(hp + 3 * (M_src + M_rcv), 0, sizeof(float) * 3 * M_src);
-        if (orV_rcv) memcpy(hp + 3 * (2 * M_src + M_rcv), orV_rcv, sizeof(float) * 3 * M_rcv);
-        else memset(hp + 3 * (2 * M_src + M_rcv), 0, sizeof(float) * 3 * M_rcv);
-        float *dp = reinterpret_cast<float *>(d + o_pos);
-        dps = dp; dpr = dp + 3 * M_src; dos = dp + 3 * (M_src + M_rcv); dor = dp + 3 * (2 * M_src + M_rcv);
-    }
-    if (s->ws_recorded) CK(cudaStreamWaitEvent(st, s->ws_busy, 0));   // earlier calls, any stream
-    CK(cudaMemcpyAsync(d, h, stage_bytes, cudaMemcpyHostToDevice, st));
-    CK(cudaEventRecord(s->stage_done, st));
-    s->stage_pending = true;
-    float *dout = host_io ? reinterpret_cast<float *>(d + o_out) : out;
-    const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + o_room);
-    s->ev_ism = s->ev_tail = false;
-    s->last_h2d = stage_bytes;
-    s->last_d2h = sizeof(int) + (host_io ? (uint64_t)M * R.n_total * sizeof(float) : 0);
-    if (s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
-    if (P.grid > 0)
-        CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + o_items),
-                              (int)P.items.size(), dps, dpr, dos, dor, dout, s->d_ctl, s->d_ctl + 1,
-                              P.em, P.nsub, P.clamp, P.grid, st));
-    if (s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
-    const int n_diff = R.n_total - R.n_ism;
-    if (s->profile && n_diff > 0) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
-    if (n_diff > 0)
-        CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + o_rirs), (int)M, n_diff, dps, dpr,
-                       dout, s->seed, s->calls, s->noise, reinterpret_cast<float *>(d + o_env), st));
-    if (s->ev_tail) CK(cudaEventRecord(s->ev[3], st));
-    s->env_off = o_env;
-    s->last_n_rir = n_diff > 0 ? M : 0;
-    s->calls++;
-    CK(cudaMemcpyAsync(s->h_ctl + 1, s->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    if (host_io)
-        CK(cudaMemcpyAsync(out, dout, (size_t)M * R.n_total * sizeof(float), cudaMemcpyDeviceToHost, st));
-    CK(cudaEventRecord(s->ws_busy, st));
-    s->ws_recorded = true;
-    if (host_io) {
-        CK(cudaStreamSynchronize(st));
-        return check_status(s);
+    R[0].n_src = M_src; R[0].n_rcv = M_rcv;
+    return simulate_rooms(s, R, M_src, M_rcv, pos_src, pos_rcv, orV_src, orV_rcv, out,
+                          (long long)M_src * M_rcv * R[0].n_total, host_io, st);
+}
+
+// Room table of a batch: offsets of sources, receivers, RIRs and output rows.
+static int build_batch(int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                       std::vector<RoomDesc> &R, long &n_src, long &n_rcv, long long &out_elems) {
+    if (n_rooms < 1 || !rooms) return fail(GPURIR_ERR_INVALID, "need at least one room");
+    R.assign(n_rooms, RoomDesc{});
+    n_src = n_rcv = 0;
+    out_elems = 0;
+    long n_rir = 0;
+    for (int i = 0; i < n_rooms; i++) {
+        const gpurir_room &g = rooms[i];
+        if (g.n_src < 1 || g.n_rcv < 1)
+            return fail(GPURIR_ERR_INVALID, "room " + std::to_string(i) + ": need a source and a receiver");
+        int rc = build_room(R[i], g.room_sz, g.beta, g.nb_img, g.Tdiff, g.Tmax, Fs, c,
+                            g.spkr_pattern, g.mic_pattern);
+        if (rc) return fail(rc, "room " + std::to_string(i) + ": " + g_err);
+        R[i].n_src = g.n_src;
+        R[i].n_rcv = g.n_rcv;
+        R[i].src_off = (int)n_src;
+        R[i].rcv_off = (int)n_rcv;
+        R[i].rir_off = (int)n_rir;
+        R[i].out_off = out_elems;
+        n_src += g.n_src;
+        n_rcv += g.n_rcv;
+        n_rir += (long)g.n_src * g.n_rcv;
+        out_elems += (long long)g.n_src * g.n_rcv * R[i].n_total;
+        if (n_rir > (1L << 30) || n_src > (1L << 30) || n_rcv > (1L << 30))
+            return fail(GPURIR_ERR_INVALID, "batch too large");
     }
     return GPURIR_OK;
 }
@@ -509,5 +609,152 @@ extern "C" int gpurir_last_transfer_bytes(gpurir_sim *s, uint64_t *h2d, uint64_t
     if (!s || !h2d || !d2h) return fail(GPURIR_ERR_INVALID, "NULL argument");
     *h2d = s->last_h2d;
     *d2h = s->last_d2h;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_batch_layout(int n_rooms, const gpurir_room *rooms, float Fs,
+                                   long long *rir_offsets) {
+    if (!rir_offsets) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    std::vector<RoomDesc> R;
+    long ns, nr;
+    long long tot;
+    int rc = build_batch(n_rooms, rooms, Fs, 343.0f, R, ns, nr, tot);
+    if (rc) return rc;
+    for (int i = 0; i < n_rooms; i++) rir_offsets[i] = R[i].out_off;
+    rir_offsets[n_rooms] = tot;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_simulate_batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
+                                            float Fs, float c, const float *d_pos_src,
+                                            const float *d_pos_rcv, const float *d_orV_src,
+                                            const float *d_orV_rcv, float *d_out, void *stream) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    if (!d_pos_src || !d_pos_rcv || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    std::vector<RoomDesc> R;
+    long ns, nr;
+    long long tot;
+    int rc = build_batch(n_rooms, rooms, Fs, c, R, ns, nr, tot);
+    if (rc) return rc;
+    for (int i = 0; i < n_rooms; i++)
+        if ((R[i].spkr != 0 && !d_orV_src) || (R[i].mic != 0 && !d_orV_rcv))
+            return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
+    return simulate_rooms(s, R, ns, nr, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_out, tot, false,
+                          reinterpret_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Captured batch: descriptors uploaded once, the launch sequence recorded in a
+// CUDA graph and replayed.  Positions and orientations are read from the same
+// device buffers at every replay, so callers may update them in place.
+// ---------------------------------------------------------------------------
+struct gpurir_batch {
+    gpurir_sim *sim = nullptr;
+    char *d = nullptr;            // descriptors + envelope + work counter + call offset
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long n_rir = 0;
+    long long out_elems = 0;
+};
+
+namespace gpurir {
+cudaError_t advance_counter_launch(uint64_t *counter, cudaStream_t st);
+}
+
+extern "C" int gpurir_batch_create(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs,
+                                   float c, const float *d_pos_src, const float *d_pos_rcv,
+                                   const float *d_orV_src, const float *d_orV_rcv, float *d_out,
+                                   gpurir_batch **out) {
+    if (!s || !out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    std::vector<RoomDesc> R;
+    long ns, nr;
+    long long tot;
+    int rc = build_batch(n_rooms, rooms, Fs, c, R, ns, nr, tot);
+    if (rc) return rc;
+    Plan P;
+    if ((rc = plan_rooms(s, R, P))) return rc;
+    const long M = (long)P.rirs.size();
+    Layout L = make_layout(P, R.size(), ns, nr, M, tot, false);
+    const size_t o_ctl = align_up(L.o_out, 256);           // work counter, then the call offset
+    const size_t bytes = o_ctl + 256;
+    std::vector<char> h(L.stage_bytes);
+    fill_stage(h.data(), L, R, P);
+    gpurir_batch *b = new gpurir_batch();
+    b->sim = s;
+    b->n_rir = M;
+    b->out_elems = tot;
+    cudaStream_t cap = nullptr;
+    cudaError_t e = cudaMalloc(&b->d, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d, h.data(), L.stage_bytes, cudaMemcpyHostToDevice);
+    uint64_t start = s->calls;
+    if (e == cudaSuccess) e = cudaMemcpy(b->d + o_ctl + 8, &start, sizeof(start), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        if (cap) cudaStreamDestroy(cap);
+        gpurir_batch_destroy(b);
+        return fail(GPURIR_ERR_CUDA, std::string("gpurir_batch_create: ") + cudaGetErrorString(e));
+    }
+    int *counter = reinterpret_cast<int *>(b->d + o_ctl);
+    uint64_t *offset = reinterpret_cast<uint64_t *>(b->d + o_ctl + 8);
+    e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        rc = enqueue_kernels(s, P, b->d, L, M, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_out,
+                             counter, offset, cap, false);
+        if (rc == GPURIR_OK && P.max_n_diff > 0) {
+            cudaError_t e2 = advance_counter_launch(offset, cap);   // next replay draws new noise
+            if (e2 != cudaSuccess) rc = fail(GPURIR_ERR_CUDA, cudaGetErrorString(e2));
+        }
+        cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
+        if (rc == GPURIR_OK && e3 != cudaSuccess) rc = fail(GPURIR_ERR_CUDA, cudaGetErrorString(e3));
+    } else {
+        rc = fail(GPURIR_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaStreamDestroy(cap);
+    if (rc == GPURIR_OK) {
+        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) rc = fail(GPURIR_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e));
+    }
+    if (rc != GPURIR_OK) {
+        gpurir_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_batch_launch(gpurir_batch *b, void *stream) {
+    if (!b || !b->exec) return fail(GPURIR_ERR_INVALID, "NULL batch");
+    CK(cudaGraphLaunch(b->exec, reinterpret_cast<cudaStream_t>(stream)));
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_batch_info(gpurir_batch *b, long long *n_rir, long long *out_elems) {
+    if (!b) return fail(GPURIR_ERR_INVALID, "NULL batch");
+    if (n_rir) *n_rir = b->n_rir;
+    if (out_elems) *out_elems = b->out_elems;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_batch_destroy(gpurir_batch *b) {
+    if (!b) return GPURIR_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d) {
+        cudaDeviceSynchronize();
+        cudaFree(b->d);
+    }
+    delete b;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_device_status(gpurir_sim *s) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    int v = 0;
+    CK(cudaMemcpy(&v, s->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v != 0) {
+        CK(cudaMemset(s->d_ctl + 1, 0, sizeof(int)));
+        return fail(GPURIR_ERR_DEVICE, "kernel rejected a work item (code " + std::to_string(v) + ")");
+    }
     return GPURIR_OK;
 }

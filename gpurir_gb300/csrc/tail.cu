@@ -20,6 +20,7 @@ struct TailLaunch {
     const float *pos_src, *pos_rcv;
     float *out;
     uint64_t seed, offset;
+    const uint64_t *offset_ptr;   // if set, the call offset is read here (captured graphs)
     int noise_kind;          // 0 logistic (reference), 1 Gaussian (Box-Muller)
     float *env_out;          // optional [n_rir][3]: A, alpha, tau_dp
 };
@@ -83,7 +84,8 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
     __syncthreads();
     const float ea = envA, eb = envB;
     const uint2 key = make_uint2((uint32_t)P.seed, (uint32_t)(P.seed >> 32));
-    const uint32_t off_lo = (uint32_t)P.offset, off_hi = (uint32_t)(P.offset >> 32);
+    const uint64_t offset = P.offset_ptr ? *P.offset_ptr : P.offset;
+    const uint32_t off_lo = (uint32_t)offset, off_hi = (uint32_t)(offset >> 32);
     const uint32_t gidx = (uint32_t)it.rir;
     float *trow = row + n_ism;
 #pragma unroll 1
@@ -117,16 +119,26 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
 
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
-                        uint64_t offset, int noise_kind, float *env_out, cudaStream_t st) {
+                        uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
+                        cudaStream_t st) {
     if (n_rir <= 0 || max_n_diff <= 0) return cudaSuccess;
     TailLaunch p;
     p.rooms = rooms; p.rirs = rirs; p.n_rir = n_rir;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.out = out;
-    p.seed = seed; p.offset = offset; p.noise_kind = noise_kind; p.env_out = env_out;
+    p.seed = seed; p.offset = offset; p.offset_ptr = offset_ptr; p.noise_kind = noise_kind;
+    p.env_out = env_out;
     const long chunks = ((long)max_n_diff + kTailChunk - 1) / kTailChunk;
     if (chunks > 65535) return cudaErrorInvalidValue;
     dim3 grid(n_rir, (unsigned)chunks);
     tail_kernel<<<grid, kTailThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+// One thread: the call offset of a captured graph advances by one per replay.
+__global__ void advance_counter_kernel(uint64_t *counter) { *counter += 1; }
+
+cudaError_t advance_counter_launch(uint64_t *counter, cudaStream_t st) {
+    advance_counter_kernel<<<1, 1, 0, st>>>(counter);
     return cudaGetLastError();
 }
 

@@ -99,6 +99,47 @@ int gpurir_simulate_rir_device(gpurir_sim *sim, const float room_sz[3], const fl
                                int mic_pattern, int M_rcv, const int nb_img[3], float Tdiff,
                                float Tmax, float Fs, float c, float *d_rir_out, void *stream);
 
+/* One room of a batch.  All rooms of a batch share Fs and c. */
+typedef struct gpurir_room {
+    float room_sz[3];      /* [m] */
+    float beta[6];         /* reflection coefficients, order x0 x1 y0 y1 z0 z1 */
+    int nb_img[3];         /* images per axis */
+    float Tdiff;           /* [s] end of the ISM part (<= Tmax) */
+    float Tmax;            /* [s] RIR length */
+    int n_src, n_rcv;      /* sources and receivers of this room */
+    int spkr_pattern, mic_pattern;
+} gpurir_room;
+
+/* Ragged output layout of a batch: rir_offsets[r] is the element offset of room
+ * r's RIRs, C order [n_src][n_rcv][nSamples_r]; rir_offsets[n_rooms] is the
+ * total.  `rir_offsets` holds n_rooms + 1 values.  gpuRIR has no batching: a
+ * batch replaces a Python loop of cuda_simulateRIR calls (src/gpuRIR_cuda.cu:766). */
+int gpurir_batch_layout(int n_rooms, const gpurir_room *rooms, float Fs, long long *rir_offsets);
+
+/* Simulate a batch of rooms in one persistent launch (device I/O, stream-ordered).
+ * Sources of room r are rows [sum of earlier n_src, +n_src) of d_pos_src (and of
+ * d_orV_src), receivers likewise; d_out is laid out by gpurir_batch_layout. */
+int gpurir_simulate_batch_device(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms, float Fs,
+                                 float c, const float *d_pos_src, const float *d_pos_rcv,
+                                 const float *d_orV_src, const float *d_orV_rcv, float *d_out,
+                                 void *stream);
+
+/* A batch planned once and captured in a CUDA graph.  gpurir_batch_launch
+ * replays it on `stream`; positions/orientations are re-read from the device
+ * buffers given at creation on every replay, and each replay draws the next
+ * noise of the handle's seed.  No counterpart in the reference. */
+typedef struct gpurir_batch gpurir_batch;
+int gpurir_batch_create(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                        const float *d_pos_src, const float *d_pos_rcv, const float *d_orV_src,
+                        const float *d_orV_rcv, float *d_out, gpurir_batch **out);
+int gpurir_batch_launch(gpurir_batch *batch, void *stream);
+int gpurir_batch_info(gpurir_batch *batch, long long *n_rir, long long *out_elems);
+int gpurir_batch_destroy(gpurir_batch *batch);
+
+/* Reads and clears the device status word that kernels set when they reject a
+ * work item (the stream-ordered entries cannot report it synchronously). */
+int gpurir_device_status(gpurir_sim *sim);
+
 /* Raw Philox4x32-10 words of the tail stream of one RIR (counter blocks
  * (j, rir_index, call_lo, call_hi), key (seed_lo, seed_hi)), into device
  * memory; for checking the stream bit-exactly against a host replay. */

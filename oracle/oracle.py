@@ -177,7 +177,7 @@ NOISE_KINDS = {"logistic": 0, "gaussian": 1}
 
 def simulate_rir(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
                  spkr_pattern="omni", mic_pattern="omni", orV_src=None, orV_rcv=None, c=343.0,
-                 seed=1234, offset=0, noise="logistic", return_parts=False):
+                 seed=1234, offset=0, noise="logistic", return_parts=False, rir_base=0):
     """FP64 restatement of cuda_simulateRIR (src/gpuRIR_cuda.cu:766-931).
 
     Returns float64 [M_src, M_rcv, nSamples]: the early part by the ISM, the rest
@@ -194,10 +194,11 @@ def simulate_rir(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
     out = ism_sum(amp.reshape(ms * mr, -1), tau.reshape(ms * mr, -1), n_ism, fs, ld=n_tot)
     A, al = env_pred(out, tdp, n_ism, fs, room_sz, beta)
     if n_diff > 0:
+        idx = np.arange(rir_base, rir_base + ms * mr, dtype=np.uint32)   # Philox stream per RIR
         lib().orc_tail(_p(A, ctypes.c_double), _p(al, ctypes.c_double),
                        _p(np.ascontiguousarray(tdp.reshape(-1)), ctypes.c_double), ms * mr,
-                       n_ism, n_diff, int(seed), int(offset), None, NOISE_KINDS[noise],
-                       _p(out, ctypes.c_double), n_tot)
+                       n_ism, n_diff, int(seed), int(offset), _p(idx, ctypes.c_uint32),
+                       NOISE_KINDS[noise], _p(out, ctypes.c_double), n_tot)
     out = out.reshape(ms, mr, n_tot)
     if return_parts:
         return out, dict(amp=amp, tau=tau, tau_dp=tdp, A=A.reshape(ms, mr),
