@@ -1,0 +1,89 @@
+"""Differentiable RIR simulation (torch.autograd) over the CUDA adjoint kernel.
+
+Gradients of a loss of the early (ISM) part with respect to the wall
+reflection coefficients, the source and receiver positions and the source and
+receiver orientations.  The backward pass recomputes image amplitudes and
+delays (nothing per image is stored by the forward pass).  The diffuse tail,
+if any, is produced by the forward pass but not differentiated.
+
+    rirs = simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv)   # packed, autograd
+    loss = ((rirs - target) ** 2).sum(); loss.backward()
+
+``rooms`` fixes the static structure (room_sz, nb_img, Tmax, Tdiff, patterns
+and the per-room source/receiver counts); beta [n_rooms, 6], pos_src
+[sum n_src, 3], pos_rcv [sum n_rcv, 3] and the optional orientations are
+float32 CUDA tensors.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib, simulator
+from .batch import _room_struct, layout
+
+
+class _IsmBatch(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, beta, pos_src, pos_rcv, orV_src, orV_rcv, spec):
+        rooms, fs, c, sim = spec
+        rooms = [dict(r, beta=b) for r, b in zip(rooms, beta.detach().cpu().numpy())]
+        table = _room_struct(rooms)
+        off = layout(rooms, fs)
+        out = torch.empty(int(off[-1]), dtype=torch.float32, device=pos_src.device)
+        st = torch.cuda.current_stream(pos_src.device).cuda_stream
+        L = _lib.load()
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        _lib.check(L.gpurir_simulate_batch_device(sim.handle, len(rooms), table, float(fs), float(c),
+                                                  ptr(pos_src), ptr(pos_rcv), ptr(orV_src),
+                                                  ptr(orV_rcv), out.data_ptr(), ctypes.c_void_p(st)),
+                   "gpurir_simulate_batch_device")
+        ctx.spec = (rooms, fs, c, sim, table)
+        ctx.save_for_backward(pos_src, pos_rcv, orV_src, orV_rcv)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        rooms, fs, c, sim, table = ctx.spec
+        pos_src, pos_rcv, orV_src, orV_rcv = ctx.saved_tensors
+        g = grad_out.contiguous()
+        dev = pos_src.device
+        gb = torch.empty((len(rooms), 6), dtype=torch.float32, device=dev) if ctx.needs_input_grad[0] else None
+        gs = torch.empty_like(pos_src) if ctx.needs_input_grad[1] else None
+        gr = torch.empty_like(pos_rcv) if ctx.needs_input_grad[2] else None
+        gos = torch.empty_like(orV_src) if orV_src is not None and ctx.needs_input_grad[3] else None
+        gor = torch.empty_like(orV_rcv) if orV_rcv is not None and ctx.needs_input_grad[4] else None
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        st = torch.cuda.current_stream(dev).cuda_stream
+        L = _lib.load()
+        _lib.check(L.gpurir_ism_backward_batch_device(
+            sim.handle, len(rooms), table, float(fs), float(c), ptr(pos_src), ptr(pos_rcv),
+            ptr(orV_src), ptr(orV_rcv), g.data_ptr(), ptr(gb), ptr(gs), ptr(gr), ptr(gos), ptr(gor),
+            ctypes.c_void_p(st)), "gpurir_ism_backward_batch_device")
+        return gb, gs, gr, gos, gor, None
+
+
+def simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, c=343.0,
+                         sim=None):
+    """Packed RIRs of a batch (float32 CUDA tensor) with autograd through the early part."""
+    for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv):
+        if t is not None and (t.dtype != torch.float32 or not t.is_cuda):
+            raise ValueError("beta, positions and orientations must be float32 CUDA tensors")
+    beta = beta.reshape(len(rooms), 6)
+    contig = lambda t: t.contiguous() if t is not None else None
+    return _IsmBatch.apply(beta, contig(pos_src), contig(pos_rcv), contig(orV_src), contig(orV_rcv),
+                           (rooms, fs, c, sim or simulator()))
+
+
+def simulate_rir_torch(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
+                       spkr_pattern="omni", mic_pattern="omni", orV_src=None, orV_rcv=None, c=343.0,
+                       sim=None):
+    """One room, simulateRIR's arguments as tensors; returns [M_src, M_rcv, nSamples]."""
+    room = dict(room_sz=np.asarray(room_sz, dtype=np.float32), beta=np.zeros(6, np.float32),
+                pos_src=np.zeros((pos_src.shape[0], 3), np.float32),
+                pos_rcv=np.zeros((pos_rcv.shape[0], 3), np.float32), nb_img=list(nb_img), Tmax=Tmax,
+                Tdiff=Tdiff, spkr_pattern=spkr_pattern, mic_pattern=mic_pattern)
+    out = simulate_batch_torch([room], fs, beta.reshape(1, 6), pos_src, pos_rcv, orV_src, orV_rcv, c,
+                               sim)
+    from .workloads import n_samples
+    return out.view(pos_src.shape[0], pos_rcv.shape[0], n_samples(Tmax, fs))

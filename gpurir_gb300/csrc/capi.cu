@@ -32,6 +32,14 @@ cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, i
 cudaError_t philox_stream_launch(uint32_t *out, long n, uint64_t seed, uint64_t offset,
                                  uint32_t rir, cudaStream_t st);
 cudaError_t probe_peaks(double *fp32_flops, double *mufu_ops, cudaStream_t st);
+size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad);
+cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
+                                const float *pos_src, const float *pos_rcv, const float *orv_src,
+                                const float *orv_rcv, const float *grad, float *item_grad,
+                                int *work_counter, int *status, int max_tseg, int grid,
+                                cudaStream_t st);
+cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
+                               int comp_lo, int n_comp, float *out, cudaStream_t st);
 }  // namespace gpurir
 
 using namespace gpurir;
@@ -756,5 +764,92 @@ extern "C" int gpurir_device_status(gpurir_sim *s) {
         CK(cudaMemset(s->d_ctl + 1, 0, sizeof(int)));
         return fail(GPURIR_ERR_DEVICE, "kernel rejected a work item (code " + std::to_string(v) + ")");
     }
+    return GPURIR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+static void csr(const std::vector<IsmItem> &items, int n_target, int IsmItem::*field, int base_sub,
+                std::vector<int> &ptr, std::vector<int> &list) {
+    ptr.assign(n_target + 1, 0);
+    for (const IsmItem &it : items) ptr[it.*field - base_sub + 1]++;
+    for (int t = 0; t < n_target; t++) ptr[t + 1] += ptr[t];
+    list.assign(items.size(), 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (size_t i = 0; i < items.size(); i++) list[fill[items[i].*field - base_sub]++] = (int)i;
+}
+
+extern "C" int gpurir_ism_backward_batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
+                                                float Fs, float c, const float *d_pos_src,
+                                                const float *d_pos_rcv, const float *d_orV_src,
+                                                const float *d_orV_rcv, const float *d_grad_rir,
+                                                float *d_grad_beta, float *d_grad_pos_src,
+                                                float *d_grad_pos_rcv, float *d_grad_orV_src,
+                                                float *d_grad_orV_rcv, void *stream) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    if (!d_pos_src || !d_pos_rcv || !d_grad_rir) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    std::vector<RoomDesc> R;
+    long ns, nr;
+    long long tot;
+    int rc = build_batch(n_rooms, rooms, Fs, c, R, ns, nr, tot);
+    if (rc) return rc;
+    for (int i = 0; i < n_rooms; i++)
+        if ((R[i].spkr != 0 && !d_orV_src) || (R[i].mic != 0 && !d_orV_rcv))
+            return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
+    Plan P;
+    if ((rc = plan_rooms(s, R, P))) return rc;
+    const int n_items = (int)P.items.size();
+    int max_tseg = 1;
+    for (const IsmItem &it : P.items) max_tseg = std::max(max_tseg, it.t_hi - it.t_lo);
+    std::vector<int> p_room, l_room, p_src, l_src, p_rcv, l_rcv;
+    csr(P.items, n_rooms, &IsmItem::room, 0, p_room, l_room);
+    csr(P.items, (int)ns, &IsmItem::src, 0, p_src, l_src);
+    csr(P.items, (int)nr, &IsmItem::rcv, 0, p_rcv, l_rcv);
+    // staging: rooms | items | csr arrays ; device adds item partials
+    size_t o_rooms = 0;
+    size_t o_items = align_up(R.size() * sizeof(RoomDesc), 256);
+    size_t o_csr = align_up(o_items + P.items.size() * sizeof(IsmItem), 256);
+    const std::vector<int> *arrs[6] = {&p_room, &l_room, &p_src, &l_src, &p_rcv, &l_rcv};
+    size_t o_arr[6], off = o_csr;
+    for (int a = 0; a < 6; a++) { o_arr[a] = off; off = align_up(off + arrs[a]->size() * sizeof(int), 256); }
+    const size_t stage_bytes = off;
+    const size_t o_ig = stage_bytes;
+    const size_t dev_bytes = align_up(o_ig + (size_t)std::max(n_items, 1) * 18 * sizeof(float), 256);
+    if ((rc = ensure_device(s, dev_bytes))) return rc;
+    if ((rc = ensure_stage(s, stage_bytes))) return rc;
+    char *h = s->h_stage;
+    memcpy(h + o_rooms, R.data(), R.size() * sizeof(RoomDesc));
+    if (n_items) memcpy(h + o_items, P.items.data(), P.items.size() * sizeof(IsmItem));
+    for (int a = 0; a < 6; a++)
+        if (!arrs[a]->empty()) memcpy(h + o_arr[a], arrs[a]->data(), arrs[a]->size() * sizeof(int));
+    char *d = s->d_ws;
+    if (s->ws_recorded) CK(cudaStreamWaitEvent(st, s->ws_busy, 0));
+    CK(cudaMemcpyAsync(d, h, stage_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(s->stage_done, st));
+    s->stage_pending = true;
+    float *ig = reinterpret_cast<float *>(d + o_ig);
+    if (n_items == 0) {
+        CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));
+    } else {
+        const int pad = 64 * P.tpl;
+        const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad);
+        if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
+        const int grid = std::min(n_items, s->num_sms);   // one 512-thread block per SM (registers)
+        CK(ism_backward_launch(P.tpl, reinterpret_cast<const RoomDesc *>(d + o_rooms),
+                               reinterpret_cast<const IsmItem *>(d + o_items), n_items, d_pos_src,
+                               d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, s->d_ctl, s->d_ctl + 1,
+                               max_tseg, grid, st));
+    }
+    const int *dp[6];
+    for (int a = 0; a < 6; a++) dp[a] = reinterpret_cast<const int *>(d + o_arr[a]);
+    if (d_grad_beta) CK(grad_reduce_launch(ig, dp[0], dp[1], n_rooms, 0, 6, d_grad_beta, st));
+    if (d_grad_pos_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)ns, 6, 3, d_grad_pos_src, st));
+    if (d_grad_pos_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)nr, 9, 3, d_grad_pos_rcv, st));
+    if (d_grad_orV_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)ns, 12, 3, d_grad_orV_src, st));
+    if (d_grad_orV_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)nr, 15, 3, d_grad_orV_rcv, st));
+    CK(cudaEventRecord(s->ws_busy, st));
+    s->ws_recorded = true;
     return GPURIR_OK;
 }

@@ -1,0 +1,428 @@
+// ism_backward.cu -- adjoint of the image-source early part for sm_103a.
+//
+// gpuRIR has no gradients.  For a loss L of the RIRs, with g[t] = dL/dh[t] over
+// the early part, each image n contributes
+//   dL/damp_n = sum_t g[t] W(t - tau_n)            (A)
+//   dL/dtau_n = -amp_n sum_t g[t] W'(t - tau_n)    (-amp B)
+// with W = Hann window x sinc, the tap of image_sample (src/gpuRIR_cuda.cu:116-121).
+// Amplitudes and delays are recomputed from the geometry (as the forward kernel
+// does), then the chain rule gives per-image contributions to
+//   beta (6 walls), source and receiver positions, source and receiver
+//   orientations,
+// summed per work item into 18 partials.  A second kernel sums the partials of
+// each room / source / receiver over a fixed item order: results are
+// deterministic (no floating-point atomics).
+//
+// Tap arithmetic (x = k - f, tau = n0 + f, per-lane constants ck, sk for the
+// window as in the forward kernel, sigma = -sin(pi f)/pi, gamma = cos(pi f)):
+//   s  = (-1)^k sigma / x,         s' = ((-1)^k gamma - s) / x
+//   w  = 0.5 + ck cos(phi) + sk sin(phi),   w' = (2 pi/Tw)(ck sin(phi) - sk cos(phi))
+//   W  = w s,   W' = w' s + w s'.
+#include "gpurir_internal.cuh"
+
+namespace gpurir {
+
+constexpr int kBThreads = 512;
+constexpr int kBWarps = kBThreads / 32;
+constexpr int kBChunk = 1024;
+constexpr int kBRounds = kBChunk / kBThreads;   // images per lane and chunk
+constexpr int kGrad = 18;                       // beta[6], src[3], rcv[3], orv_src[3], orv_rcv[3]
+
+struct BwdLaunch {
+    const RoomDesc *rooms;
+    const IsmItem *items;
+    int n_items;
+    const float *pos_src, *pos_rcv, *orv_src, *orv_rcv;
+    const float *grad;        // dL/dh, same layout as the forward output
+    float *item_grad;         // [n_items][kGrad]
+    int *work_counter;
+    int *status;
+    int max_tseg;
+    int pad;                  // g staging margin (>= taps reach)
+};
+
+__device__ __forceinline__ float rcp_approx_b(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Derivative of the polar-pattern gain with respect to cos(theta)
+// (src/gpuRIR_cuda.cu:140-145; homni is flat almost everywhere).
+__device__ __forceinline__ float pattern_slope(int pattern) {
+    switch (pattern) {
+    case P_CARD: return 0.5f;
+    case P_HYPCARD: return 0.75f;
+    case P_SUBCARD: return 0.25f;
+    case P_BIDIR: return 1.0f;
+    default: return 0.0f;
+    }
+}
+
+template <int TPL>
+__global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P) {
+    constexpr int KS = 32 * TPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *rec = reinterpret_cast<float4 *>(smem_raw);          // sigma, f, cos phi, sin phi
+    float *rec_gamma = reinterpret_cast<float *>(rec + kBChunk);  // cos(pi f)
+    int *rec_n0 = reinterpret_cast<int *>(rec_gamma + kBChunk);   // floor(tau) - t_lo
+    int *rec_idx = rec_n0 + kBChunk;                              // image index
+    float *ga = reinterpret_cast<float *>(rec_idx + kBChunk);     // A per kept image
+    float *gb = ga + kBChunk;                                     // B per kept image
+    int *wcount = reinterpret_cast<int *>(gb + kBChunk);          // [kBWarps] kept per warp
+    int *woff = wcount + kBWarps;
+    int *ctl = woff + kBWarps;                                    // [0] item, [1] kept total
+    float *red = reinterpret_cast<float *>(ctl + 4);              // [kBWarps][kGrad]
+    float *gs = red + kBWarps * kGrad;                            // staged dL/dh
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        if (tid == 0) ctl[0] = atomicAdd(P.work_counter, 1);
+        __syncthreads();
+        const int item_id = ctl[0];
+        if (item_id >= P.n_items) break;
+        const IsmItem it = P.items[item_id];
+        const RoomDesc &R = P.rooms[it.room];
+        const int t_lo = it.t_lo, t_hi = it.t_hi;
+        if (t_hi - t_lo > P.max_tseg || t_hi <= t_lo) {
+            if (tid == 0) atomicExch(P.status, DEV_BAD_ITEM);
+            __syncthreads();
+            continue;
+        }
+        // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment.
+        const int g_len = t_hi - t_lo + 2 * P.pad;
+        const float *grow = P.grad + it.out_row;
+        for (int i = tid; i < g_len; i += kBThreads) {
+            const int t = t_lo - P.pad + i;
+            gs[i] = (t >= t_lo && t < t_hi) ? grow[t] : 0.0f;
+        }
+        const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
+        const int N0 = R.nb[0], N1 = R.nb[1], N2 = R.nb[2];
+        const int n_img = R.n_img;
+        const float H = R.H, inv_h = 1.0f / H;
+        const int k_lo = (int)floorf(-H) + 1;
+        const int spkr = R.spkr, mic = R.mic;
+        const ff kfs = {R.kh, R.kl};
+        const float sx = P.pos_src[3 * it.src], sy = P.pos_src[3 * it.src + 1], sz = P.pos_src[3 * it.src + 2];
+        const float rx = P.pos_rcv[3 * it.rcv], ry = P.pos_rcv[3 * it.rcv + 1], rz = P.pos_rcv[3 * it.rcv + 2];
+        float os[3] = {0.f, 0.f, 0.f}, orr[3] = {0.f, 0.f, 0.f}, inv_os = 0.f, inv_or = 0.f;
+        if (spkr != P_OMNI) {
+            for (int d = 0; d < 3; d++) os[d] = P.orv_src[3 * it.src + d];
+            inv_os = rsqrtf(os[0] * os[0] + os[1] * os[1] + os[2] * os[2]);
+        }
+        if (mic != P_OMNI) {
+            for (int d = 0; d < 3; d++) orr[d] = P.orv_rcv[3 * it.rcv + d];
+            inv_or = rsqrtf(orr[0] * orr[0] + orr[1] * orr[1] + orr[2] * orr[2]);
+        }
+        const float keep_lo = (float)t_lo - H, keep_hi = (float)t_hi + H;
+        const float fs_c = R.kh + R.kl;   // Fs / c
+        const float dws = 3.14159265358979323846f * inv_h;   // 2 pi / Tw
+        // per-lane tap constants
+        float kf[TPL], ck[TPL], sk[TPL];
+#pragma unroll
+        for (int i = 0; i < TPL; i++) {
+            kf[i] = (float)(k_lo + lane + 32 * i);
+            float sn, cs;
+            sincospif(kf[i] * inv_h, &sn, &cs);
+            ck[i] = 0.5f * cs;
+            sk[i] = 0.5f * sn;
+        }
+        const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
+        float acc[kGrad];
+#pragma unroll
+        for (int q = 0; q < kGrad; q++) acc[q] = 0.0f;
+
+        for (int cbase = 0; cbase < n_img; cbase += kBChunk) {
+            // ---- pass A: geometry, keep images whose window meets the segment (image order)
+            int kept_mine = 0;
+            int keep_flag[kBRounds];
+            float4 r4[kBRounds];
+            float rg[kBRounds];
+            int rn0[kBRounds], ridx[kBRounds];
+#pragma unroll
+            for (int r = 0; r < kBRounds; r++) {
+                const int local = warp * (32 * kBRounds) + r * 32 + lane;
+                const int i = cbase + local;
+                keep_flag[r] = 0;
+                r4[r] = make_float4(0.f, 0.f, 1.f, 0.f);
+                rg[r] = 1.f;
+                rn0[r] = 0;
+                ridx[r] = i;
+                if (i < n_img) {
+                    const int q = i / N2, m2 = i - q * N2, m0 = q / N1, m1 = q - m0 * N1;
+                    int c0, r0, c1, r1, c2, r2;
+                    image_axis(m0, N0, c0, r0);
+                    image_axis(m1, N1, c1, r1);
+                    image_axis(m2, N2, c2, r2);
+                    const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
+                    const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
+                    const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
+                    const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
+                    const ff tau = ff_mul(ff_sqrt(d2), kfs);
+                    if (tau.hi > keep_lo && tau.hi < keep_hi) {
+                        float fl = floorf(tau.hi);
+                        int n0 = (int)fl;
+                        float f = __fadd_rn(__fsub_rn(tau.hi, fl), tau.lo);
+                        if (f < 0.0f) { n0 -= 1; f += 1.0f; }
+                        if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
+                        f = fmaxf(f, 9.094947017729282e-13f);
+                        float sp, cp, sphi, cphi;
+                        sincospif(f, &sp, &cp);
+                        sincospif(f * inv_h, &sphi, &cphi);
+                        r4[r] = make_float4(-sp * 0.318309886183790672f, f, cphi, sphi);
+                        rg[r] = cp;
+                        rn0[r] = n0 - t_lo;
+                        keep_flag[r] = 1;
+                        kept_mine++;
+                    }
+                }
+            }
+            // warp-level compaction in image order
+            int wsum = 0, my_before = 0;
+            unsigned bal[kBRounds];
+#pragma unroll
+            for (int r = 0; r < kBRounds; r++) {
+                bal[r] = __ballot_sync(0xffffffffu, keep_flag[r]);
+                wsum += __popc(bal[r]);
+            }
+            if (lane == 0) wcount[warp] = wsum;
+            __syncthreads();
+            if (tid == 0) {
+                int run = 0;
+                for (int w = 0; w < kBWarps; w++) { woff[w] = run; run += wcount[w]; }
+                ctl[1] = run;
+            }
+            __syncthreads();
+            {
+                int pos = woff[warp];
+#pragma unroll
+                for (int r = 0; r < kBRounds; r++) {
+                    if (keep_flag[r]) {
+                        const int j = pos + __popc(bal[r] & ((1u << lane) - 1u));
+                        rec[j] = r4[r];
+                        rec_gamma[j] = rg[r];
+                        rec_n0[j] = rn0[r];
+                        rec_idx[j] = ridx[r];
+                    }
+                    pos += __popc(bal[r]);
+                }
+            }
+            (void)kept_mine;
+            __syncthreads();
+            const int n_kept = ctl[1];
+            // ---- pass B: per kept image, A and B over its taps; contiguous slices per warp
+            {
+                const int per = (n_kept + kBWarps - 1) / kBWarps;
+                const int j0 = min(warp * per, n_kept), j1 = min(j0 + per, n_kept);
+                const float *gl = gs + P.pad + lane;
+                for (int j = j0; j < j1; j += 2) {
+                    float a[2] = {0.f, 0.f}, b[2] = {0.f, 0.f};
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int jj = min(j + u, j1 - 1);
+                        const float4 c = rec[jj];
+                        const float sig = c.x * lane_sign, f = c.y, cphi = c.z, sphi = c.w;
+                        const float gam = rec_gamma[jj] * lane_sign;
+                        const float *gp = gl + rec_n0[jj] + k_lo;
+#pragma unroll
+                        for (int i = 0; i < TPL; i++) {
+                            const float x = kf[i] - f;
+                            const float rx_ = rcp_approx_b(x);
+                            const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
+                            const float wd = dws * fmaf(ck[i], sphi, -sk[i] * cphi);
+                            const float s = sig * rx_;
+                            const float sd = (gam - s) * rx_;
+                            float W = w * s, Wd = fmaf(wd, s, w * sd);
+                            if (fabsf(x) >= H) { W = 0.0f; Wd = 0.0f; }
+                            const float g = gp[32 * i];
+                            a[u] = fmaf(g, W, a[u]);
+                            b[u] = fmaf(g, Wd, b[u]);
+                        }
+                    }
+                    if (j + 1 >= j1) { a[1] = 0.f; b[1] = 0.f; }
+                    // reduce 4 values over the warp with 6 shuffles
+                    const bool hi = lane & 16;
+                    float x0 = (hi ? a[1] : a[0]) + __shfl_xor_sync(0xffffffffu, hi ? a[0] : a[1], 16);
+                    float x1 = (hi ? b[1] : b[0]) + __shfl_xor_sync(0xffffffffu, hi ? b[0] : b[1], 16);
+                    const bool b3 = lane & 8;
+                    float y = (b3 ? x1 : x0) + __shfl_xor_sync(0xffffffffu, b3 ? x0 : x1, 8);
+                    y += __shfl_xor_sync(0xffffffffu, y, 4);
+                    y += __shfl_xor_sync(0xffffffffu, y, 2);
+                    y += __shfl_xor_sync(0xffffffffu, y, 1);
+                    // lanes 0 / 8 / 16 / 24 hold A(j) / B(j) / A(j+1) / B(j+1)
+                    if (lane == 0) ga[j] = y;
+                    if (lane == 8) gb[j] = y;
+                    if (j + 1 < j1) {
+                        if (lane == 16) ga[j + 1] = y;
+                        if (lane == 24) gb[j + 1] = y;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- pass C: chain rule, one kept image per lane
+            for (int j = tid; j < n_kept; j += kBThreads) {
+                const int i = rec_idx[j];
+                const int q = i / N2, m2 = i - q * N2, m0 = q / N1, m1 = q - m0 * N1;
+                int cc[3], rr[3];
+                image_axis(m0, N0, cc[0], rr[0]);
+                image_axis(m1, N1, cc[1], rr[1]);
+                image_axis(m2, N2, cc[2], rr[2]);
+                const float src[3] = {sx, sy, sz}, rcv[3] = {rx, ry, rz}, L[3] = {L0, L1, L2};
+                float v[3];
+                int e[6];
+                float pwv[6];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    v[d] = (float)(2 * cc[d]) * L[d] + (rr[d] ? -src[d] : src[d]) - rcv[d];
+                    e[2 * d] = abs(cc[d] - rr[d]);
+                    e[2 * d + 1] = abs(cc[d]);
+                    pwv[2 * d] = __ldg(&R.pw[2 * d][e[2 * d]]);
+                    pwv[2 * d + 1] = __ldg(&R.pw[2 * d + 1][e[2 * d + 1]]);
+                }
+                const float d2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+                const float inv_d = rsqrtf(d2);
+                const float att = pwv[0] * pwv[1] * pwv[2] * pwv[3] * pwv[4] * pwv[5];
+                float Ds = 1.f, Dm = 1.f, cs_ = 0.f, cm = 0.f;
+                float ms[3] = {0.f, 0.f, 0.f};   // mirrored source axis
+                if (spkr != P_OMNI) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) ms[d] = (rr[d] ? -os[d] : os[d]);
+                    cs_ = -(ms[0] * v[0] + ms[1] * v[1] + ms[2] * v[2]) * inv_d * inv_os;
+                    Ds = pattern_gain(cs_, spkr);
+                }
+                if (mic != P_OMNI) {
+                    cm = (orr[0] * v[0] + orr[1] * v[1] + orr[2] * v[2]) * inv_d * inv_or;
+                    Dm = pattern_gain(cm, mic);
+                }
+                const float g0 = 0.0795774715459476679f * inv_d;   // 1 / (4 pi d)
+                const float amp = att * Ds * Dm * g0;
+                const float GA = ga[j];
+                const float GT = -amp * gb[j];                      // dL/dtau
+                // beta: d att / d beta_w = -e_w (-beta_w)^(e_w - 1) * (other five factors)
+#pragma unroll
+                for (int w = 0; w < 6; w++) {
+                    if (e[w] > 0) {
+                        float others = 1.0f;
+#pragma unroll
+                        for (int u = 0; u < 6; u++)
+                            if (u != w) others *= pwv[u];
+                        const float datt = -(float)e[w] * __ldg(&R.pw[w][e[w] - 1]) * others;
+                        acc[w] = fmaf(GA * Ds * Dm * g0, datt, acc[w]);
+                    }
+                }
+                // d amp / d v and d tau / d v
+                const float ds = pattern_slope(spkr), dm = pattern_slope(mic);
+                float dv[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const float u = v[d] * inv_d;
+                    float damp = -amp * u * inv_d;                          // 1/d term
+                    if (spkr != P_OMNI)   // d cos_s / d v = (-ms/|o| - cos_s u) / d
+                        damp += att * g0 * Dm * ds * (-ms[d] * inv_os - cs_ * u) * inv_d;
+                    if (mic != P_OMNI)    // d cos_m / d v = (o/|o| - cos_m u) / d
+                        damp += att * g0 * Ds * dm * (orr[d] * inv_or - cm * u) * inv_d;
+                    dv[d] = GA * damp + GT * fs_c * u;
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    acc[6 + d] += rr[d] ? -dv[d] : dv[d];   // source: image coordinate (1 - 2 refl) src
+                    acc[9 + d] -= dv[d];                    // receiver
+                }
+                if (spkr != P_OMNI) {   // d cos_s / d o = (-(1-2r) v / d - cos_s o / |o|) / |o|
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        const float dcs = (-(rr[d] ? -v[d] : v[d]) * inv_d - cs_ * os[d] * inv_os) * inv_os;
+                        acc[12 + d] = fmaf(GA * att * g0 * Dm * ds, dcs, acc[12 + d]);
+                    }
+                }
+                if (mic != P_OMNI) {    // d cos_m / d o = (v / d - cos_m o / |o|) / |o|
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        const float dcm = (v[d] * inv_d - cm * orr[d] * inv_or) * inv_or;
+                        acc[15 + d] = fmaf(GA * att * g0 * Ds * dm, dcm, acc[15 + d]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // ---- item partials: warp sums, then warps in order
+#pragma unroll
+        for (int q = 0; q < kGrad; q++) {
+            float v = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp * kGrad + q] = v;
+        }
+        __syncthreads();
+        if (tid < kGrad) {
+            float s = 0.0f;
+            for (int w = 0; w < kBWarps; w++) s += red[w * kGrad + tid];
+            P.item_grad[(long)item_id * kGrad + tid] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// Sum of item partials per target, in the order of the CSR lists (deterministic).
+//   target t: components [comp_lo, comp_lo + n_comp) of the items list[ptr[t]..ptr[t+1])
+//   are summed into out[t * n_comp + c].
+__global__ void grad_reduce_kernel(const float *item_grad, const int *ptr, const int *list, int n_target,
+                                   int comp_lo, int n_comp, float *out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_target * n_comp) return;
+    const int t = e / n_comp, c = e - t * n_comp;
+    float s = 0.0f;
+    for (int p = ptr[t]; p < ptr[t + 1]; p++) s += item_grad[(long)list[p] * kGrad + comp_lo + c];
+    out[e] = s;
+}
+
+size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
+    (void)tpl;
+    return kBChunk * (sizeof(float4) + 5 * sizeof(int)) + (2 * kBWarps + 4) * sizeof(int) +
+           kBWarps * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
+}
+
+template <int TPL>
+static cudaError_t bwd_tpl(const BwdLaunch &p, int grid, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(ism_backward_kernel<TPL>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return e;
+    ism_backward_kernel<TPL><<<grid, kBThreads, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
+                                const float *pos_src, const float *pos_rcv, const float *orv_src,
+                                const float *orv_rcv, const float *grad, float *item_grad,
+                                int *work_counter, int *status, int max_tseg, int grid,
+                                cudaStream_t st) {
+    BwdLaunch p;
+    p.rooms = rooms; p.items = items; p.n_items = n_items;
+    p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
+    p.grad = grad; p.item_grad = item_grad; p.work_counter = work_counter; p.status = status;
+    p.max_tseg = max_tseg;
+    p.pad = 64 * tpl;   // >= 2 * 32 * TPL reach of the taps on either side
+    size_t smem = ism_backward_smem_bytes(tpl, max_tseg, p.pad);
+    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    switch (tpl) {
+    case 2: return bwd_tpl<2>(p, grid, smem, st);
+    case 4: return bwd_tpl<4>(p, grid, smem, st);
+    case 8: return bwd_tpl<8>(p, grid, smem, st);
+    case 12: return bwd_tpl<12>(p, grid, smem, st);
+    case 16: return bwd_tpl<16>(p, grid, smem, st);
+    case 24: return bwd_tpl<24>(p, grid, smem, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
+                               int comp_lo, int n_comp, float *out, cudaStream_t st) {
+    const int n = n_target * n_comp;
+    if (n <= 0) return cudaSuccess;
+    grad_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(item_grad, ptr, list, n_target, comp_lo,
+                                                         n_comp, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gpurir

@@ -136,6 +136,21 @@ int gpurir_batch_launch(gpurir_batch *batch, void *stream);
 int gpurir_batch_info(gpurir_batch *batch, long long *n_rir, long long *out_elems);
 int gpurir_batch_destroy(gpurir_batch *batch);
 
+/* Adjoint of the early (ISM) part of a batch.  Given dL/dRIR in the packed
+ * layout of gpurir_batch_layout (`d_grad_rir`; only the early samples are
+ * read: the diffuse tail is not differentiated), writes
+ *   d_grad_beta [n_rooms][6], d_grad_pos_src / d_grad_orV_src [sum n_src][3],
+ *   d_grad_pos_rcv / d_grad_orV_rcv [sum n_rcv][3]
+ * (each may be NULL).  Image amplitudes and delays are recomputed, not stored.
+ * Deterministic.  gpuRIR has no counterpart (it is not differentiable). */
+int gpurir_ism_backward_batch_device(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms,
+                                     float Fs, float c, const float *d_pos_src,
+                                     const float *d_pos_rcv, const float *d_orV_src,
+                                     const float *d_orV_rcv, const float *d_grad_rir,
+                                     float *d_grad_beta, float *d_grad_pos_src,
+                                     float *d_grad_pos_rcv, float *d_grad_orV_src,
+                                     float *d_grad_orV_rcv, void *stream);
+
 /* Reads and clears the device status word that kernels set when they reject a
  * work item (the stream-ordered entries cannot report it synchronously). */
 int gpurir_device_status(gpurir_sim *sim);

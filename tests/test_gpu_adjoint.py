@@ -1,0 +1,173 @@
+"""GPU checks of the adjoint kernel behind torch.autograd: gradients with respect
+to beta, source/receiver positions and orientations against FP64 torch autograd
+of the same formulas (tests/torch_ism_ref.py) and against FP64 central
+differences of the C oracle (step 1e-5).
+
+Tolerance: relative L2 error of each gradient <= 2e-4 against FP64 autograd
+(FP32 forward quantities, FP32 accumulation over ~1e5 taps)."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-4
+
+
+def _setup(seed, spkr="card", mic="hypcard", ns=2, nr=3, nb=(5, 6, 7), T=0.06, room=(4.0, 3.5, 2.8)):
+    rng = np.random.default_rng(seed)
+    room = np.array(room)
+    ps = (0.5 + rng.random((ns, 3)) * (room - 1.0)).astype(np.float32)
+    pr = (0.5 + rng.random((nr, 3)) * (room - 1.0)).astype(np.float32)
+    os_ = rng.standard_normal((ns, 3)).astype(np.float32)
+    or_ = rng.standard_normal((nr, 3)).astype(np.float32)
+    beta = rng.uniform(0.6, 0.95, 6).astype(np.float32)
+    n = oracle.n_samples(T, 16000.0)
+    g = rng.standard_normal((ns, nr, n))
+    return dict(room=room.astype(np.float32), ps=ps, pr=pr, os=os_, orv=or_, beta=beta, nb=list(nb),
+                T=T, n=n, g=g, spkr=spkr, mic=mic)
+
+
+def _ours(c):
+    import torch
+    from gpurir_gb300.autograd import simulate_rir_torch
+    t = lambda a: torch.tensor(a, device="cuda", requires_grad=True)
+    beta, ps, pr = t(c["beta"]), t(c["ps"]), t(c["pr"])
+    os_ = t(c["os"]) if c["spkr"] != "omni" else None
+    or_ = t(c["orv"]) if c["mic"] != "omni" else None
+    h = simulate_rir_torch(c["room"], beta, ps, pr, c["nb"], c["T"], 16000.0, spkr_pattern=c["spkr"],
+                           mic_pattern=c["mic"], orV_src=os_, orV_rcv=or_)
+    loss = (h.double() * torch.tensor(c["g"], device="cuda")).sum()
+    loss.backward()
+    grads = dict(beta=beta.grad, ps=ps.grad, pr=pr.grad)
+    if os_ is not None:
+        grads["os"] = os_.grad
+    if or_ is not None:
+        grads["orv"] = or_.grad
+    return {k: v.detach().cpu().numpy().astype(np.float64) for k, v in grads.items()}, h
+
+
+def _ref(c):
+    import torch
+    from torch_ism_ref import early_part
+    t = lambda a: torch.tensor(np.asarray(a, dtype=np.float64), requires_grad=True)
+    beta, ps, pr, os_, or_ = t(c["beta"]), t(c["ps"]), t(c["pr"]), t(c["os"]), t(c["orv"])
+    h = early_part(c["room"], beta, ps, pr, c["nb"], c["n"], 16000.0, spkr=c["spkr"], mic=c["mic"],
+                   orV_src=os_, orV_rcv=or_)
+    loss = (h * torch.tensor(c["g"])).sum()
+    loss.backward()
+    out = dict(beta=beta.grad, ps=ps.grad, pr=pr.grad, os=os_.grad, orv=or_.grad)
+    return {k: v.numpy() for k, v in out.items() if v is not None}, h.detach().numpy()
+
+
+@pytest.mark.parametrize("spkr,mic", [("omni", "omni"), ("card", "hypcard"), ("subcard", "bidir"),
+                                      ("hypcard", "card")])
+def test_gradients_match_fp64_autograd(built, spkr, mic):
+    c = _setup(31, spkr, mic)
+    ours, h = _ours(c)
+    ref, href = _ref(c)
+    assert rel_l2(h.detach().cpu().numpy(), href) < 1e-5
+    for k in ours:
+        e = rel_l2(ours[k], ref[k])
+        assert e < TOL, (k, e)
+
+
+def test_beta_gradient_matches_central_differences(built):
+    """dL/dbeta against FP64 central differences of the C oracle (step 1e-5)."""
+    c = _setup(32, "omni", "card", ns=1, nr=2, nb=(4, 5, 6), T=0.05)
+    ours, _ = _ours(c)
+
+    def L(beta):
+        h = oracle.simulate_rir(c["room"], beta, c["ps"], c["pr"], c["nb"], c["T"], 16000.0,
+                                mic_pattern=c["mic"], orV_rcv=c["orv"])
+        return float((h * c["g"]).sum())
+
+    fd = np.zeros(6)
+    for w in range(6):
+        e = np.zeros(6)
+        e[w] = 1e-5
+        # the oracle reads beta as float32: difference quotient over the float32 step actually taken
+        bp = (c["beta"].astype(np.float64) + e).astype(np.float32)
+        bm = (c["beta"].astype(np.float64) - e).astype(np.float32)
+        fd[w] = (L(bp) - L(bm)) / (float(bp[w]) - float(bm[w]))
+    assert rel_l2(ours["beta"], fd) < 1e-3
+
+
+def test_position_gradient_matches_central_differences(built):
+    c = _setup(33, "omni", "omni", ns=1, nr=1, nb=(3, 3, 3), T=0.04)
+    ours, _ = _ours(c)
+    fd = np.zeros(3)
+    for d in range(3):
+        hs = []
+        for sgn in (1, -1):
+            ps = c["ps"].astype(np.float64)
+            ps[0, d] += sgn * 1e-4
+            ps32 = ps.astype(np.float32)
+            h = oracle.simulate_rir(c["room"], c["beta"], ps32, c["pr"], c["nb"], c["T"], 16000.0)
+            hs.append(((h * c["g"]).sum(), float(ps32[0, d])))
+        fd[d] = (hs[0][0] - hs[1][0]) / (hs[0][1] - hs[1][1])
+    assert rel_l2(ours["ps"][0], fd) < 2e-3
+
+
+def test_batched_gradients(built):
+    """Several rooms in one launch: per-room beta, per-source and per-receiver gradients."""
+    import torch
+    from torch_ism_ref import early_part
+    from gpurir_gb300.autograd import simulate_batch_torch
+    from gpurir_gb300 import batch as B
+    rng = np.random.default_rng(34)
+    rooms, betas, ps_all, pr_all, or_all = [], [], [], [], []
+    for i in range(3):
+        cc = _setup(40 + i, "omni", "hypcard", ns=1 + i % 2, nr=2 + i, nb=(4, 5, 5), T=0.05,
+                    room=(4.0 + i, 3.5, 2.8))
+        rooms.append(dict(room_sz=cc["room"], beta=cc["beta"], pos_src=cc["ps"], pos_rcv=cc["pr"],
+                          nb_img=cc["nb"], Tmax=cc["T"], Tdiff=cc["T"], spkr_pattern="omni",
+                          mic_pattern="hypcard", orV_rcv=cc["orv"]))
+        betas.append(cc["beta"]); ps_all.append(cc["ps"]); pr_all.append(cc["pr"]); or_all.append(cc["orv"])
+    t = lambda a: torch.tensor(np.concatenate(a) if isinstance(a, list) else a, device="cuda",
+                               requires_grad=True)
+    beta, ps, pr, orv = t(np.stack(betas)), t(ps_all), t(pr_all), t(or_all)
+    out = simulate_batch_torch(rooms, 16000.0, beta, ps, pr, None, orv)
+    g = torch.tensor(rng.standard_normal(out.shape[0]), device="cuda")
+    (out.double() * g).sum().backward()
+    views = B.unpack(g.cpu().numpy(), rooms, 16000.0)
+    s0 = r0 = 0
+    for i, r in enumerate(rooms):
+        ns, nr = r["pos_src"].shape[0], r["pos_rcv"].shape[0]
+        tt = lambda a: torch.tensor(np.asarray(a, dtype=np.float64), requires_grad=True)
+        b64, p64, q64, o64 = tt(r["beta"]), tt(r["pos_src"]), tt(r["pos_rcv"]), tt(r["orV_rcv"])
+        h = early_part(r["room_sz"], b64, p64, q64, r["nb_img"], oracle.n_samples(r["Tmax"], 16000.0),
+                       16000.0, mic="hypcard", orV_rcv=o64)
+        (h * torch.tensor(views[i])).sum().backward()
+        assert rel_l2(beta.grad[i].cpu().numpy(), b64.grad.numpy()) < TOL
+        assert rel_l2(ps.grad[s0:s0 + ns].cpu().numpy(), p64.grad.numpy()) < TOL
+        assert rel_l2(pr.grad[r0:r0 + nr].cpu().numpy(), q64.grad.numpy()) < TOL
+        assert rel_l2(orv.grad[r0:r0 + nr].cpu().numpy(), o64.grad.numpy()) < TOL
+        s0 += ns
+        r0 += nr
+
+
+def test_inverse_problem_recovers_walls(built):
+    """A few Adam steps from beta = 0.8 move toward the walls that made the target."""
+    import torch
+    from gpurir_gb300.autograd import simulate_rir_torch
+    c = _setup(35, "omni", "omni", ns=2, nr=4, nb=(5, 5, 5), T=0.05)
+    ps, pr = torch.tensor(c["ps"], device="cuda"), torch.tensor(c["pr"], device="cuda")
+    true = torch.tensor(c["beta"], device="cuda")
+    with torch.no_grad():
+        target = simulate_rir_torch(c["room"], true, ps, pr, c["nb"], c["T"], 16000.0)
+    beta = torch.full((6,), 0.8, device="cuda", requires_grad=True)
+    opt = torch.optim.Adam([beta], lr=0.01)
+    first = None
+    for step in range(60):
+        opt.zero_grad()
+        loss = ((simulate_rir_torch(c["room"], beta, ps, pr, c["nb"], c["T"], 16000.0) - target) ** 2).sum()
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            beta.clamp_(0.05, 0.999)
+        first = first if first is not None else float(loss.detach())
+    assert float(loss.detach()) < 0.05 * first
+    assert float((beta - true).abs().max()) < float((0.8 - true).abs().max())

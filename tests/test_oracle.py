@@ -188,3 +188,23 @@ def test_tail_statistics():
         assert abs(z.var() - 1.0) < 0.02
         k = ((z - z.mean()) ** 4).mean() / z.var() ** 2
         assert abs(k - kurt) < 0.2
+
+
+def test_torch_fp64_reference_matches_oracle():
+    """The differentiable FP64 torch transcription used for the adjoint checks
+    agrees with the C oracle."""
+    import torch
+    from torch_ism_ref import early_part
+    rng = np.random.default_rng(7)
+    room = np.array([4.0, 3.5, 2.8], dtype=np.float32)
+    ps = (0.5 + rng.random((2, 3)) * 2.5).astype(np.float32)
+    pr = (0.5 + rng.random((2, 3)) * 2.0).astype(np.float32)
+    os_ = rng.standard_normal((2, 3)).astype(np.float32)
+    or_ = rng.standard_normal((2, 3)).astype(np.float32)
+    beta = rng.uniform(0.6, 0.95, 6).astype(np.float32)
+    t = lambda a: torch.tensor(np.asarray(a, dtype=np.float64))
+    h = early_part(room, t(beta), t(ps), t(pr), [5, 6, 7], 960, 16000.0, spkr="card", mic="bidir",
+                   orV_src=t(os_), orV_rcv=t(or_)).numpy()
+    ref = oracle.simulate_rir(room, beta, ps, pr, [5, 6, 7], 0.06, 16000.0, spkr_pattern="card",
+                              mic_pattern="bidir", orV_src=os_, orV_rcv=or_)
+    assert np.abs(h - ref).max() <= 1e-12 * np.abs(ref).max()
