@@ -70,6 +70,13 @@ SIGNATURES.update({
     "gpurir_batch_info": (c_int, [c_void_p, llptr, llptr]),
     "gpurir_batch_destroy": (c_int, [c_void_p]),
     "gpurir_device_status": (c_int, [c_void_p]),
+    "gpurir_convolutions": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_void_p]),
+    "gpurir_convolutions_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_int, c_int,
+                                           c_void_p, c_void_p]),
+    "gpurir_trajectory_device": (c_int, [c_void_p, c_void_p, c_int, c_int, iptr, c_void_p, c_int, c_int,
+                                         c_void_p, c_void_p]),
+    "gpurir_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, iptr, c_void_p, c_int, c_int,
+                                  c_void_p]),
     "gpurir_ism_backward_batch_device": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,
                                                  c_float] + [c_void_p] * 11),
 })

@@ -40,6 +40,16 @@ cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *i
                                 cudaStream_t st);
 cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
                                int comp_lo, int n_comp, float *out, cudaStream_t st);
+size_t fft_smem_bytes(int M);
+size_t fft_scratch_floats2(int M, int grid);
+cudaError_t twiddle_launch(float2 *w, int n, cudaStream_t st);
+cudaError_t segment_spectra_launch(const float *seg, int P, int S, int M, const float2 *W, float2 *Sg,
+                                   float2 *scratch, int grid, cudaStream_t st);
+cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M, const float2 *W,
+                            const float2 *Sg, float *out, long out_ld, float2 *scratch, int grid,
+                            cudaStream_t st);
+cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
+                       int L, long n_out, double *out, cudaStream_t st);
 }  // namespace gpurir
 
 using namespace gpurir;
@@ -84,6 +94,12 @@ struct gpurir_sim {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_ism = false, ev_tail = false;
     uint64_t last_h2d = 0, last_d2h = 0;
+    // convolution: twiddle tables per FFT size, and a grow-only workspace
+    std::vector<std::pair<int, float2 *>> twiddles;
+    char *d_conv = nullptr;
+    size_t d_conv_bytes = 0;
+    cudaEvent_t conv_busy = nullptr;
+    bool conv_recorded = false;
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -109,6 +125,7 @@ extern "C" int gpurir_create(int mixed_precision, int lookup_table, uint64_t see
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->stage_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ws_busy, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->conv_busy, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_ctl, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(s->d_ctl, 0, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_ctl, 4 * sizeof(int));
@@ -133,6 +150,9 @@ extern "C" int gpurir_destroy(gpurir_sim *s) {
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
     if (s->stage_done) cudaEventDestroy(s->stage_done);
     if (s->ws_busy) cudaEventDestroy(s->ws_busy);
+    if (s->conv_busy) cudaEventDestroy(s->conv_busy);
+    for (auto &t : s->twiddles) cudaFree(t.second);
+    if (s->d_conv) cudaFree(s->d_conv);
     for (int i = 0; i < 4; i++)
         if (s->ev[i]) cudaEventDestroy(s->ev[i]);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -852,4 +872,199 @@ extern "C" int gpurir_ism_backward_batch_device(gpurir_sim *s, int n_rooms, cons
     CK(cudaEventRecord(s->ws_busy, st));
     s->ws_recorded = true;
     return GPURIR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Convolution of trajectory segments with their RIRs (cuda_convolutions,
+// src/gpuRIR_cuda.cu:933-1023) and the overlap-add of simulateTrajectory.
+// ---------------------------------------------------------------------------
+static const int kFftMaxN = 1 << 24;
+
+static int fft_size(long n) {   // pow2roundup of gpuRIR (src/gpuRIR_cuda.cu:95-105), at least 8
+    long N = 8;
+    while (N < n) N <<= 1;
+    return (int)N;
+}
+
+static int get_twiddles(gpurir_sim *s, int N, cudaStream_t st, const float2 **out) {
+    for (auto &t : s->twiddles)
+        if (t.first == N) { *out = t.second; return GPURIR_OK; }
+    float2 *w = nullptr;
+    CK(cudaMalloc(&w, sizeof(float2) * N));
+    CK(twiddle_launch(w, N, st));
+    s->twiddles.push_back({N, w});
+    *out = w;
+    return GPURIR_OK;
+}
+
+static int ensure_conv(gpurir_sim *s, size_t bytes) {
+    if (bytes <= s->d_conv_bytes) return GPURIR_OK;
+    if (s->conv_recorded) CK(cudaEventSynchronize(s->conv_busy));
+    if (s->d_conv) CK(cudaFree(s->d_conv));
+    s->d_conv = nullptr;
+    s->d_conv_bytes = 0;
+    size_t want = align_up(bytes + bytes / 4, 1 << 20);
+    CK(cudaMalloc(&s->d_conv, want));
+    s->d_conv_bytes = want;
+    return GPURIR_OK;
+}
+
+struct ConvPlan {
+    int N, M, grid_seg, grid_conv;
+    size_t o_sg, o_scr, o_conv, o_win, o_in_seg, o_in_rir, bytes;
+};
+
+// Workspace layout: segment spectra | FFT scratch | conv output (optional) |
+// window table (optional) | host-staged inputs (optional).
+static int plan_conv(gpurir_sim *s, int P, int S, int R, int L, bool need_conv, bool need_win,
+                     bool stage_inputs, ConvPlan &C) {
+    if (P < 1 || R < 1 || S < 1 || L < 1) return fail(GPURIR_ERR_INVALID, "empty convolution");
+    const long n = (long)S + L - 1;
+    if (n > kFftMaxN) return fail(GPURIR_ERR_UNSUPPORTED, "segment + RIR longer than 2^24 samples");
+    C.N = fft_size(n);
+    C.M = C.N / 2;
+    const bool smem = fft_smem_bytes(C.M) > 0;
+    C.grid_seg = std::min(P, smem ? s->num_sms : 2 * s->num_sms);
+    C.grid_conv = std::min(P * R, smem ? s->num_sms : 2 * s->num_sms);
+    const int grid_scr = std::max(C.grid_seg, C.grid_conv);
+    C.o_sg = 0;
+    C.o_scr = align_up(C.o_sg + (size_t)P * (C.M + 1) * sizeof(float2), 256);
+    C.o_conv = align_up(C.o_scr + fft_scratch_floats2(C.M, grid_scr) * sizeof(float2), 256);
+    C.o_win = align_up(C.o_conv + (need_conv ? (size_t)P * R * n * sizeof(float) : 0), 256);
+    C.o_in_seg = align_up(C.o_win + (need_win ? (size_t)2 * (P + 1) * sizeof(int) : 0), 256);
+    C.o_in_rir = align_up(C.o_in_seg + (stage_inputs ? (size_t)P * S * sizeof(float) : 0), 256);
+    C.bytes = align_up(C.o_in_rir + (stage_inputs ? (size_t)P * R * L * sizeof(float) : 0), 256);
+    return ensure_conv(s, C.bytes);
+}
+
+static int run_conv(gpurir_sim *s, const ConvPlan &C, const float *d_seg, int P, int S,
+                    const float *d_rir, int R, int L, float *d_out, long out_ld, cudaStream_t st) {
+    const float2 *W = nullptr;
+    int rc = get_twiddles(s, C.N, st, &W);
+    if (rc) return rc;
+    float2 *Sg = reinterpret_cast<float2 *>(s->d_conv + C.o_sg);
+    float2 *scr = reinterpret_cast<float2 *>(s->d_conv + C.o_scr);
+    CK(segment_spectra_launch(d_seg, P, S, C.M, W, Sg, scr, C.grid_seg, st));
+    CK(rir_conv_launch(d_rir, P, R, L, S, C.M, W, Sg, d_out, out_ld, scr, C.grid_conv, st));
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_convolutions_device(gpurir_sim *s, const float *d_segments, int M_src,
+                                          int segment_len, const float *d_rir, int M_rcv, int rir_len,
+                                          float *d_out, void *stream) {
+    if (!s || !d_segments || !d_rir || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (s->conv_recorded) CK(cudaStreamWaitEvent(st, s->conv_busy, 0));
+    ConvPlan C;
+    int rc = plan_conv(s, M_src, segment_len, M_rcv, rir_len, false, false, false, C);
+    if (rc) return rc;
+    rc = run_conv(s, C, d_segments, M_src, segment_len, d_rir, M_rcv, rir_len, d_out,
+                  (long)segment_len + rir_len - 1, st);
+    if (rc) return rc;
+    CK(cudaEventRecord(s->conv_busy, st));
+    s->conv_recorded = true;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_convolutions(gpurir_sim *s, const float *source_segments, int M_src,
+                                   int segment_len, const float *RIR, int M_rcv, int RIR_len,
+                                   float *out) {
+    if (!s || !source_segments || !RIR || !out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    cudaStream_t st = s->stream;
+    if (s->conv_recorded) CK(cudaStreamWaitEvent(st, s->conv_busy, 0));
+    ConvPlan C;
+    int rc = plan_conv(s, M_src, segment_len, M_rcv, RIR_len, true, false, true, C);
+    if (rc) return rc;
+    float *dseg = reinterpret_cast<float *>(s->d_conv + C.o_in_seg);
+    float *drir = reinterpret_cast<float *>(s->d_conv + C.o_in_rir);
+    float *dout = reinterpret_cast<float *>(s->d_conv + C.o_conv);
+    const long n = (long)segment_len + RIR_len - 1;
+    CK(cudaMemcpyAsync(dseg, source_segments, sizeof(float) * M_src * segment_len, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(drir, RIR, sizeof(float) * (size_t)M_src * M_rcv * RIR_len, cudaMemcpyHostToDevice, st));
+    rc = run_conv(s, C, dseg, M_src, segment_len, drir, M_rcv, RIR_len, dout, n, st);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(out, dout, sizeof(float) * (size_t)M_src * M_rcv * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(s->conv_busy, st));
+    s->conv_recorded = true;
+    CK(cudaStreamSynchronize(st));
+    return GPURIR_OK;
+}
+
+static int check_windows(const int *w_ini, int n_pts, int seg_len, std::vector<int> &win) {
+    win.assign(2 * (n_pts + 1), 0);
+    if (w_ini[0] != 0) return fail(GPURIR_ERR_INVALID, "The first timestamp must be 0");
+    for (int p = 0; p < n_pts; p++) {
+        const int len = w_ini[p + 1] - w_ini[p];
+        if (len < 0) return fail(GPURIR_ERR_INVALID, "timestamps must not decrease");
+        if (len > seg_len) return fail(GPURIR_ERR_INVALID, "segment longer than segment_len");
+        win[p] = w_ini[p];
+        win[n_pts + 1 + p] = len;
+    }
+    win[n_pts] = w_ini[n_pts];
+    return GPURIR_OK;
+}
+
+// Shared body: segments and RIRs on the device, output [n_samples + L - 1][R] float64.
+static int trajectory_core(gpurir_sim *s, const float *d_seg, int n_pts, int seg_len,
+                           const int *w_ini, const float *d_rir, int n_rcv, int rir_len,
+                           double *d_out, const float *h_seg, const float *h_rir, cudaStream_t st) {
+    std::vector<int> win;
+    int rc = check_windows(w_ini, n_pts, seg_len, win);
+    if (rc) return rc;
+    if (s->conv_recorded) CK(cudaStreamWaitEvent(st, s->conv_busy, 0));
+    ConvPlan C;
+    const bool stage = h_seg != nullptr;
+    if ((rc = plan_conv(s, n_pts, seg_len, n_rcv, rir_len, true, true, stage, C))) return rc;
+    if (stage) {
+        float *dseg = reinterpret_cast<float *>(s->d_conv + C.o_in_seg);
+        float *drir = reinterpret_cast<float *>(s->d_conv + C.o_in_rir);
+        CK(cudaMemcpyAsync(dseg, h_seg, sizeof(float) * n_pts * seg_len, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(drir, h_rir, sizeof(float) * (size_t)n_pts * n_rcv * rir_len,
+                           cudaMemcpyHostToDevice, st));
+        d_seg = dseg;
+        d_rir = drir;
+    }
+    if ((rc = ensure_stage(s, win.size() * sizeof(int)))) return rc;
+    memcpy(s->h_stage, win.data(), win.size() * sizeof(int));
+    int *dwin = reinterpret_cast<int *>(s->d_conv + C.o_win);
+    CK(cudaMemcpyAsync(dwin, s->h_stage, win.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(s->stage_done, st));
+    s->stage_pending = true;
+    const long n = (long)seg_len + rir_len - 1;
+    float *conv = reinterpret_cast<float *>(s->d_conv + C.o_conv);
+    if ((rc = run_conv(s, C, d_seg, n_pts, seg_len, d_rir, n_rcv, rir_len, conv, n, st))) return rc;
+    CK(ola_launch(conv, n, dwin, dwin + n_pts + 1, n_pts, n_rcv, rir_len,
+                  (long)w_ini[n_pts] + rir_len - 1, d_out, st));
+    CK(cudaEventRecord(s->conv_busy, st));
+    s->conv_recorded = true;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_trajectory_device(gpurir_sim *s, const float *d_segments, int n_pts, int seg_len,
+                                        const int *w_ini, const float *d_rir, int n_rcv, int rir_len,
+                                        double *d_out, void *stream) {
+    if (!s || !d_segments || !w_ini || !d_rir || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    return trajectory_core(s, d_segments, n_pts, seg_len, w_ini, d_rir, n_rcv, rir_len, d_out, nullptr,
+                           nullptr, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gpurir_trajectory(gpurir_sim *s, const float *segments, int n_pts, int seg_len,
+                                 const int *w_ini, const float *rir, int n_rcv, int rir_len,
+                                 double *out) {
+    if (!s || !segments || !w_ini || !rir || !out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    const long n_out = (long)w_ini[n_pts] + rir_len - 1;
+    if (n_pts < 1 || n_out < 1) return fail(GPURIR_ERR_INVALID, "empty trajectory");
+    double *dout = nullptr;
+    CK(cudaMallocAsync(reinterpret_cast<void **>(&dout), sizeof(double) * n_out * n_rcv, s->stream));
+    int rc = trajectory_core(s, segments, n_pts, seg_len, w_ini, rir, n_rcv, rir_len, dout, segments,
+                             rir, s->stream);
+    if (rc == GPURIR_OK) {
+        cudaError_t e = cudaMemcpyAsync(out, dout, sizeof(double) * n_out * n_rcv, cudaMemcpyDeviceToHost,
+                                        s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) rc = fail(GPURIR_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFreeAsync(dout, s->stream);
+    cudaStreamSynchronize(s->stream);
+    return rc;
 }

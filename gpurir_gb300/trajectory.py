@@ -28,5 +28,49 @@ def segment_signal(source_signal, n_pts, timestamps=None, fs=None):
     return segments.astype('float32', order='C', copy=False), w_ini, w_len
 
 
-def simulate_trajectory(source_signal, RIRs, timestamps=None, fs=None):
-    raise NotImplementedError("simulateTrajectory: the GPU convolution kernels are not built yet")
+def gpu_conv(source_segments, RIRs, sim=None):
+    """Batched convolutions of gpuRIR_bind.gpu_conv (src/python_bind.cpp:90-119):
+    float32 [P, S] x float32 [P, R, L] -> float32 [P, R, S + L - 1]."""
+    from . import _lib, simulator
+    sim = sim or simulator()
+    seg = np.ascontiguousarray(np.asarray(source_segments, dtype=np.float32))
+    rir = np.ascontiguousarray(np.asarray(RIRs, dtype=np.float32))
+    if seg.ndim != 2 or rir.ndim != 3 or seg.shape[0] != rir.shape[0]:
+        raise ValueError("source_segments [P, S] and RIRs [P, R, L] with the same P")
+    P, S = seg.shape
+    _, R, L = rir.shape
+    out = np.empty((P, R, S + L - 1), dtype=np.float32)
+    _lib.check(_lib.load().gpurir_convolutions(sim.handle, seg.ctypes.data, P, S, rir.ctypes.data, R, L,
+                                               out.ctypes.data), "gpurir_convolutions")
+    return out
+
+
+def simulate_trajectory(source_signal, RIRs, timestamps=None, fs=None, sim=None):
+    """simulateTrajectory: float64 [len(signal) + L - 1, R] (numpy), or a float64
+    CUDA tensor when RIRs is a CUDA tensor (then everything stays on the device)."""
+    from . import _lib, simulator
+    sim = sim or simulator()
+    n_pts = RIRs.shape[0]
+    seg, w_ini, w_len = segment_signal(source_signal, n_pts, timestamps, fs)
+    w = np.ascontiguousarray(w_ini.astype(np.int32))
+    L = _lib.load()
+    if hasattr(RIRs, "is_cuda") and RIRs.is_cuda:
+        import torch
+        rir = RIRs.to(torch.float32).contiguous()
+        dseg = torch.from_numpy(seg).to(rir.device)
+        _, R, Lr = rir.shape
+        out = torch.empty((int(w[-1]) + Lr - 1, R), dtype=torch.float64, device=rir.device)
+        st = torch.cuda.current_stream(rir.device).cuda_stream
+        import ctypes
+        _lib.check(L.gpurir_trajectory_device(sim.handle, dseg.data_ptr(), n_pts, seg.shape[1],
+                                              w.ctypes.data_as(_lib.iptr), rir.data_ptr(), R, Lr,
+                                              out.data_ptr(), ctypes.c_void_p(st)),
+                   "gpurir_trajectory_device")
+        return out
+    rir = np.ascontiguousarray(np.asarray(RIRs, dtype=np.float32))
+    _, R, Lr = rir.shape
+    out = np.empty((int(w[-1]) + Lr - 1, R), dtype=np.float64)
+    _lib.check(L.gpurir_trajectory(sim.handle, seg.ctypes.data, n_pts, seg.shape[1],
+                                   w.ctypes.data_as(_lib.iptr), rir.ctypes.data, R, Lr,
+                                   out.ctypes.data), "gpurir_trajectory")
+    return out

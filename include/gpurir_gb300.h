@@ -151,6 +151,33 @@ int gpurir_ism_backward_batch_device(gpurir_sim *sim, int n_rooms, const gpurir_
                                      float *d_grad_pos_rcv, float *d_grad_orV_src,
                                      float *d_grad_orV_rcv, void *stream);
 
+/* Batched FFT convolutions of trajectory segments with their RIRs, host
+ * buffers.  Replaces gpuRIR_cuda::cuda_convolutions, src/gpuRIR_cuda.cu:933-1023
+ * (called by gpuRIR_bind::gpu_conv, src/python_bind.cpp:90-119), same argument
+ * order: source_segments [M_src][segment_len], RIR [M_src][M_rcv][RIR_len];
+ * the caller owns `out`, float32 [M_src][M_rcv][segment_len + RIR_len - 1]. */
+int gpurir_convolutions(gpurir_sim *sim, const float *source_segments, int M_src, int segment_len,
+                        const float *RIR, int M_rcv, int RIR_len, float *out);
+
+/* Same on device buffers, stream-ordered. */
+int gpurir_convolutions_device(gpurir_sim *sim, const float *d_segments, int M_src, int segment_len,
+                               const float *d_rir, int M_rcv, int rir_len, float *d_out, void *stream);
+
+/* simulateTrajectory's convolutions and overlap-add in one call (gpuRIR does
+ * the overlap-add in a Python loop, gpuRIR/__init__.py:215-219).  Segment p
+ * starts at sample w_ini[p] of the signal and is w_ini[p+1] - w_ini[p] long
+ * (w_ini: host array of n_pts + 1 values, w_ini[0] = 0, w_ini[n_pts] = signal
+ * length); segments [n_pts][seg_len] zero-padded; RIRs [n_pts][n_rcv][rir_len].
+ * Output float64 [w_ini[n_pts] + rir_len - 1][n_rcv], summed over points in
+ * increasing order (compensated float32 sums).  Device buffers, stream-ordered. */
+int gpurir_trajectory_device(gpurir_sim *sim, const float *d_segments, int n_pts, int seg_len,
+                             const int *w_ini, const float *d_rir, int n_rcv, int rir_len,
+                             double *d_out, void *stream);
+
+/* Same with host buffers (blocking). */
+int gpurir_trajectory(gpurir_sim *sim, const float *segments, int n_pts, int seg_len, const int *w_ini,
+                      const float *rir, int n_rcv, int rir_len, double *out);
+
 /* Reads and clears the device status word that kernels set when they reject a
  * work item (the stream-ordered entries cannot report it synchronously). */
 int gpurir_device_status(gpurir_sim *sim);
