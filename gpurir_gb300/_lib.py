@@ -77,6 +77,9 @@ SIGNATURES.update({
                                          c_void_p, c_void_p]),
     "gpurir_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, iptr, c_void_p, c_int, c_int,
                                   c_void_p]),
+    "gpurir_simulate_ism_noalloc": (c_int, [fptr, fptr, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                            c_int, c_int, c_int, iptr, c_float, c_float, c_float,
+                                            c_void_p, c_void_p]),
     "gpurir_ism_backward_batch_device": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,
                                                  c_float] + [c_void_p] * 11),
 })

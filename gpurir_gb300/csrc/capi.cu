@@ -1068,3 +1068,24 @@ extern "C" int gpurir_trajectory(gpurir_sim *s, const float *segments, int n_pts
     cudaStreamSynchronize(s->stream);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Helpers shared with the fixed-scratch entry point (ism_noalloc.cu).
+// ---------------------------------------------------------------------------
+namespace gpurir {
+int describe_room(RoomDesc &R, const float room[3], const float beta[6], const int nb[3], float Tdiff,
+                  float Tmax, float Fs, float c, int spkr, int mic) {
+    return build_room(R, room, beta, nb, Tdiff, Tmax, Fs, c, spkr, mic);
+}
+
+int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub) {
+    Plan P;
+    int rc = plan_window(H, P, max_nsub);
+    tpl = P.tpl;
+    em = P.em;
+    clamp = P.clamp;
+    return rc;
+}
+
+int set_last_error(int code, const char *msg) { return fail(code, msg); }
+}  // namespace gpurir

@@ -178,6 +178,26 @@ int gpurir_trajectory_device(gpurir_sim *sim, const float *d_segments, int n_pts
 int gpurir_trajectory(gpurir_sim *sim, const float *segments, int n_pts, int seg_len, const int *w_ini,
                       const float *rir, int n_rcv, int rir_len, double *out);
 
+/* Early part of one room's RIRs without allocating any memory.  No counterpart
+ * in the reference.  For callers that must not call cudaMalloc while they run:
+ * real-time audio threads (cudaMalloc may block on a device synchronisation),
+ * hosts with a fixed device-memory budget, work recorded under global stream
+ * capture.  The kernel's scratch is a fixed ~260 KB array in this library,
+ * held on every GPU that loads it until the process exits; calls are limited to
+ * 8192 RIRs x segments (M_src * M_rcv <= 8192) and fail with GPURIR_ERR_INVALID
+ * beyond.  Computes the image-source part only, as gpurir_simulate_rir_device
+ * with Tdiff = Tmax = T: d_rir_out is [M_src][M_rcv][gpurir_n_samples(T, Fs)].
+ * The first call on a device looks up the scratch address (cudaGetSymbolAddress);
+ * make it before any stream capture.  Host arguments are copied from pageable
+ * memory, so the call waits for earlier work on `stream`.  Every call shares the
+ * one scratch array: calls whose GPU work overlaps (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int gpurir_simulate_ism_noalloc(const float room_sz[3], const float beta[6], const float *d_pos_src,
+                                int M_src, const float *d_pos_rcv, const float *d_orV_src,
+                                const float *d_orV_rcv, int spkr_pattern, int mic_pattern, int M_rcv,
+                                const int nb_img[3], float T, float Fs, float c, float *d_rir_out,
+                                void *stream);
+
 /* Reads and clears the device status word that kernels set when they reject a
  * work item (the stream-ordered entries cannot report it synchronously). */
 int gpurir_device_status(gpurir_sim *sim);
