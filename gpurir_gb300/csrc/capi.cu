@@ -17,14 +17,15 @@
 #include "../../include/gpurir_gb300.h"
 
 namespace gpurir {
-size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub);
-int ism_forward_max_nsub(int tpl, int em, size_t smem_budget);
+size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub, int mode, int tw);
+int ism_forward_max_nsub(int tpl, int em, size_t smem_budget, int mode, int tw);
 int ism_forward_pick_tpl(float H);
-int ism_forward_blocks_per_sm(int tpl, size_t smem);
+int ism_forward_blocks_per_sm(int tpl, size_t smem, int mode);
 cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
-                               int em, int max_nsub, int clamp, int grid, cudaStream_t st);
+                               int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
+                               int tw);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
@@ -313,6 +314,7 @@ static int ensure_stage(gpurir_sim *s, size_t bytes) {
 
 struct Plan {
     int tpl, em, nsub, grid, clamp;
+    int mode = 0, tw = 0;   // tap evaluation mode (0 FP32, 1 mixed precision, 2 LUT), window length
     int max_n_diff;
     std::vector<IsmItem> items;
     std::vector<IsmItem> rirs;
@@ -320,6 +322,7 @@ struct Plan {
 
 // Launch geometry shared by every room of a launch (all rooms use one Fs).
 static int plan_window(float H, Plan &P, int &max_nsub) {
+    P.tw = (int)std::lround(2.0 * H);
     P.tpl = ism_forward_pick_tpl(H);
     if (P.tpl < 0) return fail(GPURIR_ERR_UNSUPPORTED, "window too long (Fs above ~190 kHz)");
     const int sub = 32 * P.tpl;
@@ -328,9 +331,9 @@ static int plan_window(float H, Plan &P, int &max_nsub) {
         const int k_lo = (int)std::floor(-H) + 1, nk = (int)std::floor(H) - k_lo + 1;
         P.clamp = (nk != sub || H != std::floor(H)) ? 1 : 0;
     }
-    max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget);
+    max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudget, P.mode, P.tw);
     if (max_nsub < 4)   // long windows (high Fs): one block per SM with the whole shared memory
-        max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudgetLarge);
+        max_nsub = ism_forward_max_nsub(P.tpl, P.em, kSmemBudgetLarge, P.mode, P.tw);
     if (max_nsub < 1) return fail(GPURIR_ERR_UNSUPPORTED, "window too long for shared memory");
     return GPURIR_OK;
 }
@@ -341,6 +344,7 @@ static int plan_window(float H, Plan &P, int &max_nsub) {
 // estimate of their cost, largest first (longest-processing-time order).
 static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     int max_nsub = 0;
+    P.mode = s->lut ? 2 : (s->mp ? 1 : 0);
     int rc = plan_window(R[0].H, P, max_nsub);
     if (rc) return rc;
     const int sub = 32 * P.tpl;
@@ -398,8 +402,8 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     for (auto &w : work) P.items.push_back(w.second);
     P.grid = 0;
     if (P.items.empty()) return GPURIR_OK;
-    size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub);
-    int bps = ism_forward_blocks_per_sm(P.tpl, smem);
+    size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub, P.mode, P.tw);
+    int bps = ism_forward_blocks_per_sm(P.tpl, smem, P.mode);
     if (bps < 1) return fail(GPURIR_ERR_CUDA, "ISM kernel does not fit on an SM");
     P.grid = (int)std::min<long>((long)P.items.size(), (long)s->num_sms * bps);
     return GPURIR_OK;
@@ -450,7 +454,7 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
-                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st));
+                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw));
     if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
     if (record && s->profile && P.max_n_diff > 0) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
     if (P.max_n_diff > 0)
@@ -1079,7 +1083,7 @@ int describe_room(RoomDesc &R, const float room[3], const float beta[6], const i
 }
 
 int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub) {
-    Plan P;
+    Plan P;   // FP32 mode
     int rc = plan_window(H, P, max_nsub);
     tpl = P.tpl;
     em = P.em;

@@ -22,6 +22,8 @@
 // since sin(pi (k - f)) = -(-1)^k sin(pi f): one sinpi per image, one MUFU.RCP
 // per tap, and the Hann window by the angle-sum identity from per-lane
 // constants and a per-image (cos, sin) pair (image_sample, :116-121).
+#include <cuda_fp16.h>
+
 #include "gpurir_internal.cuh"
 
 namespace gpurir {
@@ -47,7 +49,19 @@ struct IsmLaunch {
     int em;                           // pad words before/after the buffers
     int max_nsub;                     // sub-ranges this launch's smem holds
     int clamp;                        // taps may fall outside |x| < H: clamp the window
+    int tw;                           // window length in samples (LUT mode table)
 };
+
+// Evaluation modes of the taps (template parameter MODE):
+//   kModeF32  FP32 Hann window by the angle-sum identity (default)
+//   kModeMP   mixed precision: the window evaluated in packed half2, reciprocal
+//             and accumulation in FP32 (gpuRIR's activateMixedPrecision,
+//             src/gpuRIR_cuda.cu:488-553 evaluates in half2 and also accumulates in half2)
+//   kModeLUT  gpuRIR's lookup table (src/gpuRIR_cuda.cu:236-239, 578-616): Hann x sinc
+//             sampled 16x per sample, linear interpolation with an 8-bit fractional
+//             weight as texture filtering applies it, support |x| < floor(Tw/2)
+constexpr int kModeF32 = 0, kModeMP = 1, kModeLUT = 2;
+constexpr int kLutOversamp = 16;
 
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
@@ -61,42 +75,78 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // phi = 2 pi f / Tw: the bracketed factors are per-lane constants (ck, sk) and
 // (cos phi, sin phi) comes with the image, so a tap costs one FADD, two FFMA,
 // one MUFU.RCP, one FMUL and the shared-memory accumulate.
-template <int TPL, bool CLAMP>
+template <int TPL, bool CLAMP, int MODE>
 __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], const float (&ck)[TPL],
-                                             const float (&sk)[TPL], float al, float4 r, float H) {
-    const float f = r.y, cphi = r.z, sphi = r.w;
+                                             const float (&sk)[TPL], float al, float4 r, float H,
+                                             const float2 *lut, int lut_cols) {
+    const float f = r.y;
+    if (MODE == kModeF32) {
+        const float cphi = r.z, sphi = r.w;
 #pragma unroll
-    for (int i = 0; i < TPL; i++) {
-        const float x = kf[i] - f;
-        const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
-        float v = w * rcp_approx(x);
-        if (CLAMP) v = fabsf(x) < H ? v : 0.0f;
-        p[32 * i] = fmaf(al, v, p[32 * i]);
+        for (int i = 0; i < TPL; i++) {
+            const float x = kf[i] - f;
+            const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
+            float v = w * rcp_approx(x);
+            if (CLAMP) v = fabsf(x) < H ? v : 0.0f;
+            p[32 * i] = fmaf(al, v, p[32 * i]);
+        }
+    } else if (MODE == kModeMP) {
+        const __half2 cphi = __float2half2_rn(r.z), sphi = __float2half2_rn(r.w);
+        const __half2 half = __float2half2_rn(0.5f);
+#pragma unroll
+        for (int i = 0; i < TPL; i += 2) {
+            const __half2 ck2 = __floats2half2_rn(ck[i], ck[i + 1]);
+            const __half2 sk2 = __floats2half2_rn(sk[i], sk[i + 1]);
+            const float2 w = __half22float2(__hfma2(ck2, cphi, __hfma2(sk2, sphi, half)));
+            const float x0 = kf[i] - f, x1 = kf[i + 1] - f;
+            float v0 = w.x * rcp_approx(x0), v1 = w.y * rcp_approx(x1);
+            if (CLAMP) { v0 = fabsf(x0) < H ? v0 : 0.0f; v1 = fabsf(x1) < H ? v1 : 0.0f; }
+            p[32 * i] = fmaf(al, v0, p[32 * i]);
+            p[32 * (i + 1)] = fmaf(al, v1, p[32 * (i + 1)]);
+        }
+    } else {
+        // record: al = amp, r.z = 8-bit weight, r.w = table index of tap k = 0
+        const float alpha = r.z;
+        const int base = __float_as_int(r.w);
+        const float2 *row = lut + (base & (kLutOversamp - 1)) * lut_cols;
+        const int col0 = base >> 4;
+#pragma unroll
+        for (int i = 0; i < TPL; i++) {
+            const float x = kf[i] - f;
+            int col = col0 + (int)kf[i];
+            const bool in = fabsf(x) < H && col >= 0 && col < lut_cols;
+            col = min(max(col, 0), lut_cols - 1);
+            const float2 t = row[col];
+            const float v = in ? fmaf(alpha, t.y - t.x, t.x) : 0.0f;
+            p[32 * i] = fmaf(al, v, p[32 * i]);
+        }
     }
 }
 
-template <int TPL, bool CLAMP>
+template <int TPL, bool CLAMP, int MODE>
 __device__ __forceinline__ void scatter_list(float *bs, int origin, const float4 *rec, const short *rec_n0,
                                              const unsigned short *perm, int j0, int j1,
                                              const float (&kf)[TPL], const float (&ck)[TPL],
-                                             const float (&sk)[TPL], float lane_sign, float H) {
+                                             const float (&sk)[TPL], float lane_sign, float H,
+                                             const float2 *lut, int lut_cols) {
     int j = j0;
 #pragma unroll 1
     for (; j + 1 < j1; j += 2) {   // two images per trip: half the loop bookkeeping
         const int ia = perm[j], ib = perm[j + 1];
         const float4 a = rec[ia], b = rec[ib];
         const int na = rec_n0[ia], nb = rec_n0[ib];
-        scatter_taps<TPL, CLAMP>(bs + (na - origin), kf, ck, sk, a.x * lane_sign, a, H);
-        scatter_taps<TPL, CLAMP>(bs + (nb - origin), kf, ck, sk, b.x * lane_sign, b, H);
+        scatter_taps<TPL, CLAMP, MODE>(bs + (na - origin), kf, ck, sk, a.x * lane_sign, a, H, lut, lut_cols);
+        scatter_taps<TPL, CLAMP, MODE>(bs + (nb - origin), kf, ck, sk, b.x * lane_sign, b, H, lut, lut_cols);
     }
     if (j < j1) {
         const int ia = perm[j];
         const float4 a = rec[ia];
-        scatter_taps<TPL, CLAMP>(bs + (rec_n0[ia] - origin), kf, ck, sk, a.x * lane_sign, a, H);
+        scatter_taps<TPL, CLAMP, MODE>(bs + (rec_n0[ia] - origin), kf, ck, sk, a.x * lane_sign, a, H, lut,
+                                       lut_cols);
     }
 }
 
-template <int TPL>
+template <int TPL, int MODE>
 __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     constexpr int KS = 32 * TPL;   // taps per image, rounded up to the warp
     constexpr int SUB = KS;        // sub-range length
@@ -117,6 +167,32 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     float *buf = reinterpret_cast<float *>(ctl + 8);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
+    // LUT mode: the table after the largest buffers + pool of this launch, rows of
+    // (T[16 col + row], T[16 col + row + 1]) pairs so that lanes read consecutive words.
+    const int lut_cols = P.tw + 1;
+    float2 *lut = reinterpret_cast<float2 *>(
+        buf + ((2 * P.em + P.max_nsub * BUF + kPool * (2 * P.em + BUF) + 1) & ~1));
+    if (MODE == kModeLUT) {
+        // T[j] = Hann x sinc at (j - 8 Tw) / 16, as src/gpuRIR_cuda.cu:578-592 tabulates it
+        const int center = 8 * P.tw, lut_len = 16 * P.tw + 1;
+        const float PIf = 3.141592654f, twf = (float)P.tw;
+        for (int e = tid; e < kLutOversamp * lut_cols; e += kThreads) {
+            const int row = e / lut_cols, col = e - row * lut_cols;
+            float v[2];
+            for (int u = 0; u < 2; u++) {
+                const int j = kLutOversamp * col + row + u;
+                v[u] = 0.0f;
+                if (j < lut_len) {
+                    const float x = (float)abs(j - center) / (float)kLutOversamp;
+                    const float sc = (x == 0.0f) ? 1.0f : sinf(PIf * x) / (PIf * x);
+                    v[u] = 0.5f * (1.0f + cosf(2.0f * PIf * x / twf)) * sc;
+                }
+            }
+            lut[row * lut_cols + col] = make_float2(v[0], v[1]);
+        }
+        __syncthreads();
+    }
+    const float h_lut = (float)(P.tw / 2);   // gpuRIR's LUT support |t - tau| < Tw/2 (integer)
 
     for (;;) {
         if (tid == 0) ctl[0] = atomicAdd(P.work_counter, 1);
@@ -224,8 +300,21 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     if (f < 0.0f) { n0 -= 1; f += 1.0f; }
                     if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
                     f = fmaxf(f, 9.094947017729282e-13f);   // 2^-40: keeps x = k - f != 0
-                    a = -amp * sinpif(f) * 0.318309886183790672f;
-                    sincospif(f * inv_h, &sphi, &cphi);   // phi = 2 pi f / Tw
+                    if (MODE == kModeLUT) {
+                        // texture coordinate of tap k: 16 (k - f) + 8 Tw; weight on 8 fractional
+                        // bits.  16 f and its fractional part are exact in float32, so the weight
+                        // is quantised from an exact fraction (forming 8 Tw - 16 f first would not be).
+                        const float g = 16.0f * f, gi = floorf(g), gf = g - gi;
+                        int base = 8 * P.tw - (int)gi - (gf > 0.0f ? 1 : 0);
+                        float alpha = gf > 0.0f ? rintf((1.0f - gf) * 256.0f) * (1.0f / 256.0f) : 0.0f;
+                        if (alpha >= 1.0f) { base += 1; alpha = 0.0f; }
+                        a = amp;
+                        cphi = alpha;
+                        sphi = __int_as_float(base);
+                    } else {
+                        a = -amp * sinpif(f) * 0.318309886183790672f;
+                        sincospif(f * inv_h, &sphi, &cphi);   // phi = 2 pi f / Tw
+                    }
                     if (amp != 0.0f && tau.hi > keep_lo && tau.hi < keep_hi) {
                         int rel = n0 - t_lo;
                         sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
@@ -349,10 +438,15 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     float *bs = (k == 0 ? buf + s * BUF : pool + (pool_base[s] + k - 1) * slot_words) +
                                 P.em + lane;
                     const int origin = s * SUB;   // record n0 is relative to t_lo
-                    if (P.clamp)
-                        scatter_list<TPL, true>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, lane_sign, H);
+                    if (MODE == kModeLUT)   // table values carry their sign: no lane sign
+                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, 1.0f,
+                                                      h_lut, lut, lut_cols);
+                    else if (P.clamp)
+                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk,
+                                                      lane_sign, H, lut, lut_cols);
                     else
-                        scatter_list<TPL, false>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, lane_sign, H);
+                        scatter_list<TPL, false, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk,
+                                                       lane_sign, H, lut, lut_cols);
                 }
             }
             __syncthreads();
@@ -387,17 +481,18 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub) {
+size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub, int mode, int tw) {
     const int ks = 32 * tpl;
+    size_t words = (size_t)(2 * em + max_nsub * 2 * ks) + (size_t)kPool * (2 * em + 2 * ks);
     size_t fixed = kChunk * (sizeof(float4) + sizeof(short) + sizeof(unsigned short) + 1) +
-                   (kWarps * kMaxSub + 3 * kMaxSub + kMaxItems + kPool + 8) * sizeof(int) +
-                   (size_t)kPool * (2 * em + 2 * ks) * sizeof(float);
-    return fixed + (size_t)(2 * em + max_nsub * 2 * ks) * sizeof(float);
+                   (kWarps * kMaxSub + 3 * kMaxSub + kMaxItems + kPool + 8) * sizeof(int);
+    size_t lut = mode == kModeLUT ? (size_t)kLutOversamp * (tw + 1) * sizeof(float2) + sizeof(float) : 0;
+    return fixed + words * sizeof(float) + lut;
 }
 
-int ism_forward_max_nsub(int tpl, int em, size_t smem_budget) {
+int ism_forward_max_nsub(int tpl, int em, size_t smem_budget, int mode, int tw) {
     const int ks = 32 * tpl;
-    size_t fixed = ism_forward_smem_bytes(tpl, em, 0);
+    size_t fixed = ism_forward_smem_bytes(tpl, em, 0, mode, tw);
     if (smem_budget <= fixed) return 0;
     long n = (long)((smem_budget - fixed) / (sizeof(float) * 2 * ks));
     return (int)(n < kMaxSub ? n : kMaxSub);
@@ -413,24 +508,25 @@ int ism_forward_pick_tpl(float H) {
     return -1;
 }
 
-template <int TPL>
+template <int TPL, int MODE>
 static cudaError_t launch_tpl(const IsmLaunch &p, int grid, size_t smem, cudaStream_t st) {
     static bool attr_set = false;   // per process; the attribute is per function
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(ism_forward_kernel<TPL>,
+        cudaError_t e = cudaFuncSetAttribute(ism_forward_kernel<TPL, MODE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    ism_forward_kernel<TPL><<<grid, kThreads, smem, st>>>(p);
+    ism_forward_kernel<TPL, MODE><<<grid, kThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
 
-int ism_forward_blocks_per_sm(int tpl, size_t smem) {
+template <int MODE>
+static int occupancy(int tpl, size_t smem) {
     int n = 0;
     switch (tpl) {
-#define OCC(T) case T: cudaFuncSetAttribute(ism_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ism_forward_kernel<T>, kThreads, smem); break;
+#define OCC(T) case T: cudaFuncSetAttribute(ism_forward_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ism_forward_kernel<T, MODE>, kThreads, smem); break;
         OCC(2) OCC(4) OCC(8) OCC(12) OCC(16) OCC(24)
 #undef OCC
     default: return 0;
@@ -438,25 +534,45 @@ int ism_forward_blocks_per_sm(int tpl, size_t smem) {
     return n;
 }
 
+int ism_forward_blocks_per_sm(int tpl, size_t smem, int mode) {
+    switch (mode) {
+    case kModeF32: return occupancy<kModeF32>(tpl, smem);
+    case kModeMP: return occupancy<kModeMP>(tpl, smem);
+    case kModeLUT: return occupancy<kModeLUT>(tpl, smem);
+    default: return 0;
+    }
+}
+
+template <int MODE>
+static cudaError_t launch_mode(int tpl, const IsmLaunch &p, int grid, size_t smem, cudaStream_t st) {
+    switch (tpl) {
+    case 2: return launch_tpl<2, MODE>(p, grid, smem, st);
+    case 4: return launch_tpl<4, MODE>(p, grid, smem, st);
+    case 8: return launch_tpl<8, MODE>(p, grid, smem, st);
+    case 12: return launch_tpl<12, MODE>(p, grid, smem, st);
+    case 16: return launch_tpl<16, MODE>(p, grid, smem, st);
+    case 24: return launch_tpl<24, MODE>(p, grid, smem, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
-                               int em, int max_nsub, int clamp, int grid, cudaStream_t st) {
+                               int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
+                               int tw) {
     IsmLaunch p;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
     p.out = out; p.work_counter = work_counter; p.status = status;
-    p.em = em; p.max_nsub = max_nsub; p.clamp = clamp;
-    size_t smem = ism_forward_smem_bytes(tpl, em, max_nsub);
+    p.em = em; p.max_nsub = max_nsub; p.clamp = clamp; p.tw = tw;
+    size_t smem = ism_forward_smem_bytes(tpl, em, max_nsub, mode, tw);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    switch (tpl) {
-    case 2: return launch_tpl<2>(p, grid, smem, st);
-    case 4: return launch_tpl<4>(p, grid, smem, st);
-    case 8: return launch_tpl<8>(p, grid, smem, st);
-    case 12: return launch_tpl<12>(p, grid, smem, st);
-    case 16: return launch_tpl<16>(p, grid, smem, st);
-    case 24: return launch_tpl<24>(p, grid, smem, st);
+    switch (mode) {
+    case kModeF32: return launch_mode<kModeF32>(tpl, p, grid, smem, st);
+    case kModeMP: return launch_mode<kModeMP>(tpl, p, grid, smem, st);
+    case kModeLUT: return launch_mode<kModeLUT>(tpl, p, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -18,12 +18,13 @@
 #include "../../include/gpurir_gb300.h"
 
 namespace gpurir {
-size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub);
-int ism_forward_blocks_per_sm(int tpl, size_t smem);
+size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub, int mode, int tw);
+int ism_forward_blocks_per_sm(int tpl, size_t smem, int mode);
 cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
-                               int em, int max_nsub, int clamp, int grid, cudaStream_t st);
+                               int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
+                               int tw);
 int describe_room(RoomDesc &R, const float room[3], const float beta[6], const int nb[3], float Tdiff,
                   float Tmax, float Fs, float c, int spkr, int mic);
 int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub);
@@ -135,8 +136,9 @@ extern "C" int gpurir_simulate_ism_noalloc(const float room_sz[3], const float b
         return set_last_error(GPURIR_ERR_INVALID,
                               "gpurir_simulate_ism_noalloc: RIRs x segments above 8192 (fixed scratch limit)");
     const int nsub = (int)((tseg + sub - 1) / sub);
-    const size_t smem = ism_forward_smem_bytes(tpl, em, nsub);
-    const int bps = ism_forward_blocks_per_sm(tpl, smem);
+    const int tw = (int)std::lround(2.0 * R.H);
+    const size_t smem = ism_forward_smem_bytes(tpl, em, nsub, 0, tw);
+    const int bps = ism_forward_blocks_per_sm(tpl, smem, 0);
     if (bps < 1) return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: kernel does not fit");
     const long n_items = M * n_seg;
     const int grid = (int)std::min<long>(n_items, (long)sms * bps);
@@ -152,7 +154,7 @@ extern "C" int gpurir_simulate_ism_noalloc(const float room_sz[3], const float b
     if (cudaGetLastError() != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: prepare launch failed");
     if (ism_forward_launch(tpl, d_room, d_items, (int)n_items, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
-                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st) != cudaSuccess)
+                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st, 0, tw) != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: kernel launch failed");
     return GPURIR_OK;
 }

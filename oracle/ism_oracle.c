@@ -164,6 +164,52 @@ void orc_ism_sum(const double *amp, const double *tau, long M, long N, int nISM,
     }
 }
 
+/*
+ * Lookup-table variant of the early part, restating gpuRIR's LUT path:
+ * the table of create_sinc_texture_lut (src/gpuRIR_cuda.cu:578-592: Hann x sinc
+ * at 16 samples per sample, lut_len = 16 Tw + 1, float arithmetic), the fetch
+ * coordinate of image_sample_lut (:236-239: 16 (t - tau) + lut_len/2 + 0.5,
+ * support |t - tau| < Tw/2 in integer division) and linear texture filtering
+ * with the weight held on 8 fractional bits (rounded to nearest here).
+ */
+void orc_ism_sum_lut(const double *amp, const double *tau, long M, long N, int nISM, float Fs,
+                     double *rir, long ld)
+{
+    const int Tw = orc_window_len(Fs);
+    const int lut_len = Tw * 16 + 1, center = lut_len / 2, H = Tw / 2;
+    const float PIf = 3.141592654f;
+    float *T = (float *)malloc(sizeof(float) * (size_t)(lut_len + 1));
+    for (int i = 0; i <= center; i++) {
+        float x = (float)i / 16;
+        float sc = (x == 0.0f) ? 1.0f : sinf(PIf * x) / (PIf * x);
+        float hn = 0.5f * (1.0f + cosf(2.0f * PIf * x / Tw));
+        T[center + i] = hn * sc;
+        T[center - i] = hn * sc;
+    }
+    T[lut_len] = 0.0f;
+    for (long m = 0; m < M; m++) {
+        double *h = rir + m * ld;
+        for (int t = 0; t < nISM; t++) h[t] = 0.0;
+        for (long i = 0; i < N; i++) {
+            double a = amp[m * N + i], ta = tau[m * N + i];
+            long t0 = (long)floor(ta - H);
+            if (t0 < 0) t0 = 0;
+            for (long t = t0; t < nISM && (double)t < ta + H; t++) {
+                double x = (double)t - ta;
+                if (fabs(x) >= H) continue;
+                double xb = 16.0 * x + center;
+                long j = (long)floor(xb);
+                double al = nearbyint((xb - (double)j) * 256.0) / 256.0;
+                if (al >= 1.0) { j += 1; al = 0.0; }
+                double t0v = (j >= 0 && j < lut_len) ? T[j] : 0.0;
+                double t1v = (j + 1 >= 0 && j + 1 < lut_len) ? T[j + 1] : 0.0;
+                h[t] += a * (t0v + al * (t1v - t0v));
+            }
+        }
+    }
+    free(T);
+}
+
 /* Sabine reverberation time from the walls, src/gpuRIR_cuda.cu:123-130. */
 double orc_sabine_t60(const float room[3], const float beta[6])
 {

@@ -54,6 +54,8 @@ def lib():
             L.orc_ism_sum.argtypes = [dp, dp, ctypes.c_long, ctypes.c_long, ctypes.c_int,
                                       ctypes.c_float, dp, ctypes.c_long]
             L.orc_ism_sum.restype = None
+            L.orc_ism_sum_lut.argtypes = L.orc_ism_sum.argtypes
+            L.orc_ism_sum_lut.restype = None
             L.orc_sabine_t60.argtypes = [fp, fp]
             L.orc_sabine_t60.restype = ctypes.c_double
             L.orc_env_pred.argtypes = [dp, ctypes.c_long, dp, ctypes.c_long, ctypes.c_int,
@@ -135,6 +137,19 @@ def ism_sum(amp, tau, n_ism, fs, ld=None):
     out = np.zeros((M, ld))
     lib().orc_ism_sum(_p(amp, ctypes.c_double), _p(tau, ctypes.c_double), M, N, int(n_ism),
                       float(np.float32(fs)), _p(out, ctypes.c_double), ld)
+    return out
+
+
+def ism_sum_lut(amp, tau, n_ism, fs, ld=None):
+    """Early part by gpuRIR's lookup-table semantics (FP64 sums), [M, ld]."""
+    amp = np.ascontiguousarray(amp, dtype=np.float64)
+    tau = np.ascontiguousarray(tau, dtype=np.float64)
+    N = amp.shape[-1]
+    M = amp.size // N
+    ld = n_ism if ld is None else ld
+    out = np.zeros((M, ld))
+    lib().orc_ism_sum_lut(_p(amp, ctypes.c_double), _p(tau, ctypes.c_double), M, N, int(n_ism),
+                          float(np.float32(fs)), _p(out, ctypes.c_double), ld)
     return out
 
 

@@ -1,0 +1,69 @@
+"""The two other evaluation modes of gpuRIR's API on the GPU.
+
+activateMixedPrecision: half2 window, FP32 reciprocal and accumulation; the
+  early part within 2e-3 relative L2 of the FP64 oracle.
+activateLUT: gpuRIR's lookup-table semantics (16x oversampled Hann x sinc,
+  8-bit interpolation weight, support |t - tau| < Tw/2 in integers); within
+  1e-5 relative L2 of the oracle's restatement of those semantics, and within
+  the table's own accuracy (5e-3) of the exact FP64 result.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(seed, fs=16000.0):
+    rng = np.random.default_rng(seed)
+    room = np.array([5.0, 4.0, 3.0], np.float32)
+    ps = (0.5 + rng.random((3, 3)) * 4.0 * np.array([1, 0.75, 0.5])).astype(np.float32)
+    pr = (0.5 + rng.random((4, 3)) * 3.0 * np.array([1, 0.9, 0.6])).astype(np.float32)
+    orv = rng.standard_normal((4, 3)).astype(np.float32)
+    return room, rng.uniform(0.7, 0.95, 6).astype(np.float32), ps, pr, orv
+
+
+def _run(mode, seed, fs=16000.0, nb=(7, 7, 9), T=0.12):
+    import gpurir_gb300 as G
+    room, beta, ps, pr, orv = _scene(seed, fs)
+    sim = G.Simulator()
+    if mode == "mp":
+        assert sim.activate_mixed_precision(True)
+    elif mode == "lut":
+        assert sim.activate_lut(True)
+    out = sim.simulate_rir(room, beta, ps, pr, None, orv, 0, 2, nb, T, T, fs)
+    amp, tau, _ = oracle.amp_tau(room, beta, ps, pr, nb, fs, mic_pattern="card", orV_rcv=orv)
+    n = oracle.n_samples(T, fs)
+    exact = oracle.ism_sum(amp.reshape(12, -1), tau.reshape(12, -1), n, fs)
+    lut = oracle.ism_sum_lut(amp.reshape(12, -1), tau.reshape(12, -1), n, fs)
+    return out.reshape(12, -1), exact, lut
+
+
+@pytest.mark.parametrize("fs", [16000.0, 44100.0])
+def test_mixed_precision_within_2e3(built, fs):
+    out, exact, _ = _run("mp", 50, fs)
+    e = rel_l2(out, exact)
+    assert e <= 2e-3, e
+
+
+@pytest.mark.parametrize("fs", [16000.0, 22050.0, 44100.0])
+def test_lut_mode_matches_gpuRIR_lut_semantics(built, fs):
+    out, exact, lut = _run("lut", 51, fs)
+    assert rel_l2(out, lut) <= 1e-5
+    assert rel_l2(lut, exact) <= 5e-3
+    assert rel_l2(out, exact) <= 5e-3
+
+
+def test_mode_flags_exclude_each_other(built):
+    import gpurir_gb300 as G
+    sim = G.Simulator()
+    assert sim.modes() == dict(mixed_precision=False, lut=False)
+    sim.activate_lut(True)
+    sim.activate_mixed_precision(True)
+    assert sim.modes() == dict(mixed_precision=True, lut=False)
+    sim.activate_lut(True)
+    assert sim.modes() == dict(mixed_precision=False, lut=True)
+    sim.activate_lut(False)
+    assert sim.modes() == dict(mixed_precision=False, lut=False)
