@@ -48,6 +48,8 @@ def _args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the batched / adjoint / trajectory measurements")
     return p.parse_args()
 
 
@@ -161,6 +163,109 @@ def _traffic(workload):
             return json.load(f).get(workload)
     except (OSError, ValueError):
         return None
+
+
+def _timed(fn, steps, stream, flush=None):
+    """Median device time (ms) of fn() over `steps` runs, CUDA events on `stream`."""
+    import torch
+    ts = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ts.sort()
+    return ts[len(ts) // 2]
+
+
+def run_extras(G, flush, stream):
+    """The metric's other parts: batched vs plain forward (512 uneven rooms), forward +
+    adjoint step vs forward (16 rooms x 32 RIRs), trajectory filtering (400 points)."""
+    import torch
+    from gpurir_gb300 import batch as B, workloads
+    out = {}
+    # -- batched rooms: one captured launch vs one call per room
+    rooms = workloads.batched_rooms()
+    fs = 16000.0
+    n_rir = sum(r["pos_src"].shape[0] * r["pos_rcv"].shape[0] for r in rooms)
+    sim = G.Simulator(seed=7)
+    plan = B.BatchPlan(rooms, fs, sim=sim)
+    for _ in range(2):
+        plan.launch(stream.cuda_stream)
+    t_batch = _timed(lambda: plan.launch(stream.cuda_stream), 10, stream, flush)
+    dev = stream.device
+    per_room = []
+    for r in rooms:
+        d = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
+        o = torch.empty((r["pos_src"].shape[0], r["pos_rcv"].shape[0],
+                         workloads.n_samples(r["Tmax"], fs)), device=dev)
+        per_room.append((r, d(r["pos_src"]), d(r["pos_rcv"]), o))
+
+    def plain():
+        for r, ps, pr, o in per_room:
+            sim.simulate_rir_device(r["room_sz"], r["beta"], ps, pr, None, None, 0, 0, r["nb_img"],
+                                    r["Tdiff"], r["Tmax"], fs, 343.0, o, stream.cuda_stream)
+
+    plain()
+    t_plain = _timed(plain, 3, stream, flush)
+    upd = sum(workloads.windowed_updates_torch(dict(r, fs=fs)) for r in rooms)
+    out["batched_rooms"] = {
+        "rooms": len(rooms), "rirs": n_rir, "windowed_updates": upd,
+        "batched_ms": t_batch, "batched_rirs_per_s": n_rir / (t_batch * 1e-3),
+        "batched_updates_per_s": upd / (t_batch * 1e-3),
+        "plain_loop_ms": t_plain, "plain_loop_rirs_per_s": n_rir / (t_plain * 1e-3),
+        "batched_over_plain": t_plain / t_batch,
+        "note": "batched = one CUDA-graph replay of all 512 rooms; plain = one device-API call "
+                "per room on the same stream"}
+    # -- forward + adjoint step of the inverse problem
+    from gpurir_gb300.autograd import simulate_batch_torch
+    inv = workloads.inverse_problem()
+    beta = torch.tensor(np.stack([r["beta"] for r in inv]), device=dev, requires_grad=True)
+    ps = torch.tensor(np.concatenate([r["pos_src"] for r in inv]), device=dev, requires_grad=True)
+    pr = torch.tensor(np.concatenate([r["pos_rcv"] for r in inv]), device=dev, requires_grad=True)
+    orv = torch.tensor(np.concatenate([r["orV_rcv"] for r in inv]), device=dev)
+    target = simulate_batch_torch(inv, fs, beta.detach() * 0.99, ps.detach(), pr.detach(), None, orv,
+                                  sim=sim).detach()
+
+    def fwd():
+        with torch.no_grad():
+            simulate_batch_torch(inv, fs, beta, ps, pr, None, orv, sim=sim)
+
+    def fwd_bwd():
+        loss = ((simulate_batch_torch(inv, fs, beta, ps, pr, None, orv, sim=sim) - target) ** 2).sum()
+        loss.backward()
+
+    for _ in range(3):
+        fwd(); fwd_bwd()
+    t_f = _timed(fwd, 20, stream, flush)
+    t_fb = _timed(fwd_bwd, 20, stream, flush)
+    out["inverse_problem"] = {"rirs": 16 * 32, "forward_ms": t_f, "forward_adjoint_ms": t_fb,
+                              "adjoint_over_forward": t_fb / t_f,
+                              "note": "grads of an L2 loss w.r.t. beta[16,6], pos_src[64,3], "
+                                      "pos_rcv[128,3]; includes the host round trip of beta"}
+    # -- trajectory: RIRs simulated on the device, then convolution + overlap-add
+    tr = workloads.trajectory()
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
+    tps, tpr = d(tr["pos_src"]), d(tr["pos_rcv"])
+    rirs = torch.empty((400, 8, 12800), device=dev)
+    from gpurir_gb300.trajectory import simulate_trajectory
+    sim.simulate_rir_device(tr["room_sz"], tr["beta"], tps, tpr, None, None, 0, 0, tr["nb_img"],
+                            tr["Tdiff"], tr["Tmax"], fs, 343.0, rirs, stream.cuda_stream)
+    simulate_trajectory(tr["signal"], rirs, sim=sim)
+    t_rir = _timed(lambda: sim.simulate_rir_device(tr["room_sz"], tr["beta"], tps, tpr, None, None, 0, 0,
+                                                   tr["nb_img"], tr["Tdiff"], tr["Tmax"], fs, 343.0,
+                                                   rirs, stream.cuda_stream), 10, stream, flush)
+    t_conv = _timed(lambda: simulate_trajectory(tr["signal"], rirs, sim=sim), 10, stream, flush)
+    conv_bytes = 4 * (400 * 8 * 12800 + 400 * 400 + 2 * 400 * 8 * (400 + 12799)) + 8 * 8 * (160000 + 12799)
+    out["trajectory"] = {"rir_ms": t_rir, "convolution_ola_ms": t_conv,
+                         "conv_hbm_gbs": conv_bytes / (t_conv * 1e-3) / 1e9,
+                         "note": "400 points x 8 mics, 12800-sample RIRs, 10 s signal; segments "
+                                 "uploaded from host memory inside the timed call"}
+    return out
 
 
 def run_gpu(a):
@@ -286,6 +391,8 @@ def run_gpu(a):
             "e2e": {"value": e2e_value, "unit": "RIRs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3},
             "roofline": roofline, "clocks": clk, "gpu_launches": 2 * a.steps}
+    if world == 1 and not a.no_extras:
+        line["workloads"] = run_extras(G, flush, stream)
     if world == 1 and not a.no_cpu_baseline:
         scene_cpu = workloads.mic_array()
         threads = os.cpu_count() or 1

@@ -137,3 +137,35 @@ def windowed_updates(scene, chunk=1 << 22):
         total += int(np.maximum(hi - lo + 1, 0).sum())
     M = ps.shape[0] * pr.shape[0]
     return total, M * int(np.prod(nb)) * n_ism
+
+
+def windowed_updates_torch(scene, device="cuda"):
+    """windowed_updates computed with torch (FP64) on `device`, for large scenes."""
+    import torch
+    room = torch.tensor(np.asarray(scene["room_sz"], dtype=np.float32).astype(np.float64), device=device)
+    nb = [int(x) for x in np.asarray(scene["nb_img"]).reshape(3)]
+    fs = float(np.float32(scene["fs"]))
+    c = float(np.float32(scene.get("c", 343.0)))
+    tdiff = scene.get("Tdiff") or scene["Tmax"]
+    n_ism = n_samples(tdiff, fs)
+    H = int(round(float(np.float32(8e-3) * np.float32(fs)))) / 2.0
+    ps = torch.tensor(np.asarray(scene["pos_src"], dtype=np.float64), device=device).reshape(-1, 3)
+    pr = torch.tensor(np.asarray(scene["pos_rcv"], dtype=np.float64), device=device).reshape(-1, 3)
+    off, sg = [], []
+    for d in range(3):
+        k = torch.arange(nb[d], device=device, dtype=torch.float64) - (nb[d] // 2)
+        cl = torch.ceil(k / 2.0)
+        r = torch.fmod(k, 2).abs()
+        off.append(2 * cl * room[d])
+        sg.append(1 - 2 * r)
+    total = 0
+    for s in ps:
+        for rv in pr:
+            comp = [off[d] + sg[d] * s[d] - rv[d] for d in range(3)]
+            d2 = (comp[0][:, None, None] ** 2 + comp[1][None, :, None] ** 2 +
+                  comp[2][None, None, :] ** 2)
+            tau = torch.sqrt(d2) * (fs / c)
+            lo = torch.clamp(torch.floor(tau - H) + 1, min=0)
+            hi = torch.clamp(torch.ceil(tau + H) - 1, max=n_ism - 1)
+            total += int(torch.clamp(hi - lo + 1, min=0).sum().item())
+    return total
