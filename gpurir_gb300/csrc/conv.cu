@@ -36,9 +36,10 @@ __global__ void twiddle_kernel(float2 *w, int n) {
 
 // In-block complex FFT of M points (power of two) from buf0; returns the buffer
 // that holds the result.  INV conjugates the twiddles (unnormalised inverse).
-// W is the size-N table, N = 2M: the M-point twiddle exp(-2 pi i m/M) = W[2m].
-template <bool INV>
-__device__ float2 *block_fft(float2 *buf0, float2 *buf1, int M, const float2 *__restrict__ W) {
+// tw[m] = exp(-2 pi i m / M) for m < 3M/4 (shared memory, or the global table
+// read with stride 2 when TS = 2: the size-N table holds exp(-2 pi i m/M) at 2m).
+template <bool INV, int TS>
+__device__ float2 *block_fft(float2 *buf0, float2 *buf1, int M, const float2 *tw) {
     float2 *src = buf0, *dst = buf1;
     int Ns = 1;
     int log2M = 31 - __clz(M);
@@ -59,9 +60,9 @@ __device__ float2 *block_fft(float2 *buf0, float2 *buf1, int M, const float2 *__
             const int k = j & (Ns - 1);
             float2 v0 = src[j], v1 = src[j + q], v2 = src[j + 2 * q], v3 = src[j + 3 * q];
             if (Ns > 1) {
-                float2 w1 = __ldg(&W[2 * (k * tstep)]);
-                float2 w2 = __ldg(&W[2 * (2 * k * tstep)]);
-                float2 w3 = __ldg(&W[2 * (3 * k * tstep)]);
+                float2 w1 = tw[TS * (k * tstep)];
+                float2 w2 = tw[TS * (2 * k * tstep)];
+                float2 w3 = tw[TS * (3 * k * tstep)];
                 if (INV) { w1 = cconj(w1); w2 = cconj(w2); w3 = cconj(w3); }
                 v1 = cmul(v1, w1);
                 v2 = cmul(v2, w2);
@@ -82,16 +83,48 @@ __device__ float2 *block_fft(float2 *buf0, float2 *buf1, int M, const float2 *__
     return src;
 }
 
+// Twiddles of one block.  In shared memory (M <= kSmemFftMax): twM[m] =
+// exp(-2 pi i m/M), m < 3M/4, and twN[k] = exp(-2 pi i k/N), k <= M/2, copied from
+// the global size-N table once per block; beyond that the global table is read
+// directly (stride 2 for the M-point twiddles).
+struct Twiddles {
+    const float2 *m;   // M-point twiddles
+    int ms;            // index stride into m
+    const float2 *n;   // N-point twiddles, k <= M/2
+};
+
+__device__ Twiddles load_twiddles(float2 *sm_tw, int M, const float2 *W, bool in_smem) {
+    if (!in_smem) return Twiddles{W, 2, W};
+    float2 *twm = sm_tw, *twn = sm_tw + 3 * M / 4;
+    for (int m = threadIdx.x; m < 3 * M / 4; m += blockDim.x) twm[m] = __ldg(&W[2 * m]);
+    for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) twn[k] = __ldg(&W[k]);
+    __syncthreads();
+    return Twiddles{twm, 1, twn};
+}
+
+__device__ __forceinline__ float2 *fft_fwd(float2 *a, float2 *b, int M, const Twiddles &T) {
+    return T.ms == 1 ? block_fft<false, 1>(a, b, M, T.m) : block_fft<false, 2>(a, b, M, T.m);
+}
+__device__ __forceinline__ float2 *fft_inv(float2 *a, float2 *b, int M, const Twiddles &T) {
+    return T.ms == 1 ? block_fft<true, 1>(a, b, M, T.m) : block_fft<true, 2>(a, b, M, T.m);
+}
+
+// exp(-2 pi i k/N) and exp(-2 pi i (M - k)/N) = -conj(exp(-2 pi i k/N)), 0 <= k <= M/2
+__device__ __forceinline__ void twiddle_pair(const Twiddles &T, int k, float2 &wk, float2 &wm) {
+    wk = T.n[k];
+    wm = make_float2(-wk.x, wk.y);
+}
+
 // Forward real FFT of the zero-padded length-`len` row x into X[0..M] (M + 1 bins),
 // scaled by `scale`.  z (M complex) is packed from x; work buffers a, b.
-__device__ void real_fft_row(const float *x, int len, int M, const float2 *W, float2 *a, float2 *b,
+__device__ void real_fft_row(const float *x, int len, int M, const Twiddles &T, float2 *a, float2 *b,
                              float2 *X, float scale) {
     for (int n = threadIdx.x; n < M; n += blockDim.x) {
         const int i0 = 2 * n, i1 = 2 * n + 1;
         a[n] = make_float2(i0 < len ? x[i0] : 0.0f, i1 < len ? x[i1] : 0.0f);
     }
     __syncthreads();
-    float2 *Z = block_fft<false>(a, b, M, W);
+    float2 *Z = fft_fwd(a, b, M, T);
     for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
         const int km = (M - k) & (M - 1);
         const float2 zk = Z[k], zm = Z[km];
@@ -99,8 +132,8 @@ __device__ void real_fft_row(const float *x, int len, int M, const float2 *W, fl
         const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
         const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
         const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);   // bins M - k
-        const float2 wk = __ldg(&W[k]);
-        const float2 wm = (k == 0) ? make_float2(-1.0f, 0.0f) : __ldg(&W[M - k]);
+        float2 wk, wm;
+        twiddle_pair(T, k, wk, wm);
         const float2 xk = cadd(ze, cmul(wk, zo));
         const float2 xm = cadd(ze2, cmul(wm, zo2));
         X[k] = make_float2(xk.x * scale, xk.y * scale);
@@ -116,8 +149,9 @@ __global__ void __launch_bounds__(kFftThreads) segment_spectra_kernel(
     const bool in_smem = M <= kSmemFftMax;
     float2 *a = in_smem ? sm : scratch + (size_t)blockIdx.x * 2 * M;
     float2 *b = a + M;
+    const Twiddles T = load_twiddles(sm + 2 * M, M, W, in_smem);
     for (int p = blockIdx.x; p < P; p += gridDim.x)
-        real_fft_row(seg + (size_t)p * S, S, M, W, a, b, Sg + (size_t)p * (M + 1), 1.0f / (float)M);
+        real_fft_row(seg + (size_t)p * S, S, M, T, a, b, Sg + (size_t)p * (M + 1), 1.0f / (float)M);
 }
 
 // One block per (point p, receiver r): conv[p][r][0..S+L-1) = segment p * RIR (p, r).
@@ -128,6 +162,7 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
     const bool in_smem = M <= kSmemFftMax;
     float2 *a = in_smem ? sm : scratch + (size_t)blockIdx.x * 2 * M;
     float2 *b = a + M;
+    const Twiddles T = load_twiddles(sm + 2 * M, M, W, in_smem);
     const int n_out = S + L - 1;
     for (int pr = blockIdx.x; pr < P * R; pr += gridDim.x) {
         const int p = pr / R;
@@ -137,7 +172,7 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
             a[n] = make_float2(i0 < L ? x[i0] : 0.0f, i1 < L ? x[i1] : 0.0f);
         }
         __syncthreads();
-        float2 *Z = block_fft<false>(a, b, M, W);
+        float2 *Z = fft_fwd(a, b, M, T);
         float2 *Y = (Z == a) ? b : a;   // the other buffer receives the inverse input
         const float2 *sp = Sg + (size_t)p * (M + 1);
         for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
@@ -146,8 +181,8 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
             const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
             const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
             const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
-            const float2 wk = __ldg(&W[k]);
-            const float2 wm = (k == 0) ? make_float2(-1.0f, 0.0f) : __ldg(&W[M - k]);
+            float2 wk, wm;
+            twiddle_pair(T, k, wk, wm);
             // spectra of the RIR at bins k and M - k, times the segment spectrum
             const float2 yk = cmul(cadd(ze, cmul(wk, zo)), __ldg(&sp[k]));
             const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), __ldg(&sp[M - k]));
@@ -164,7 +199,7 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
         }
         __syncthreads();
         float2 *other = (Y == a) ? b : a;
-        float2 *z = block_fft<true>(Y, other, M, W);
+        float2 *z = fft_inv(Y, other, M, T);
         float *o = out + (size_t)pr * out_ld;
         for (int n = threadIdx.x; n < M; n += blockDim.x) {
             const float2 v = z[n];
@@ -180,10 +215,9 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
 // Compensated FP32 sum (two-sum), written as float64.
 __global__ void ola_kernel(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P,
                            int R, int L, long n_out, double *out) {
-    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_out * R) return;
-    const long t = e / R;
-    const int r = (int)(e - t * R);
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;   // consecutive t: coalesced reads
+    const int r = blockIdx.y;
+    if (t >= n_out) return;
     // first point whose window may reach t: w_ini[p] + w_len[p] + L - 1 > t; points are sorted by w_ini
     int lo = 0, hi = P;   // smallest p with w_ini[p] + w_len[p] + L - 1 > t
     while (lo < hi) {
@@ -204,7 +238,10 @@ __global__ void ola_kernel(const float *conv, long conv_ld, const int *w_ini, co
     out[t * R + r] = (double)s + (double)comp;
 }
 
-size_t fft_smem_bytes(int M) { return M <= kSmemFftMax ? 2 * (size_t)M * sizeof(float2) : 0; }
+// data (2 M) + M-point twiddles (3M/4) + N-point twiddles (M/2 + 1)
+size_t fft_smem_bytes(int M) {
+    return M <= kSmemFftMax ? (2 * (size_t)M + 3 * (size_t)M / 4 + (size_t)M / 2 + 1) * sizeof(float2) : 0;
+}
 size_t fft_scratch_floats2(int M, int grid) { return M <= kSmemFftMax ? 0 : (size_t)grid * 2 * M; }
 
 cudaError_t twiddle_launch(float2 *w, int n, cudaStream_t st) {
@@ -216,10 +253,10 @@ static cudaError_t set_fft_smem() {
     static bool done = false;
     if (done) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(segment_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(2 * kSmemFftMax * sizeof(float2)));
+                                         (int)fft_smem_bytes(kSmemFftMax));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(rir_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(2 * kSmemFftMax * sizeof(float2)));
+                                 (int)fft_smem_bytes(kSmemFftMax));
     done = e == cudaSuccess;
     return e;
 }
@@ -244,10 +281,10 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
 
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
                        int L, long n_out, double *out, cudaStream_t st) {
-    const long n = n_out * R;
-    if (n <= 0) return cudaSuccess;
-    ola_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(conv, conv_ld, w_ini, w_len, P, R, L, n_out,
-                                                            out);
+    if (n_out <= 0 || R <= 0) return cudaSuccess;
+    if (R > 65535) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((n_out + 255) / 256), (unsigned)R);
+    ola_kernel<<<grid, 256, 0, st>>>(conv, conv_ld, w_ini, w_len, P, R, L, n_out, out);
     return cudaGetLastError();
 }
 
