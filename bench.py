@@ -347,6 +347,7 @@ def run_gpu(a):
         host_step()
         e2e_s += time.perf_counter() - t0
     h2d, d2h = sim.last_transfer_bytes()
+    direct = sim.last_output_direct()
     if world > 1:
         t = torch.tensor([e2e_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -389,7 +390,9 @@ def run_gpu(a):
             "updates_per_s": updates * world * a.steps / (total_ms * 1e-3),
             "kernel_ms": {"ism_forward": ism_avg, "tail": sum(tail_ms) / len(tail_ms)},
             "e2e": {"value": e2e_value, "unit": "RIRs/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3,
+                    "d2h": "kernel stores into the pinned host buffer over NVLink-C2C" if direct
+                           else "cudaMemcpyAsync after the kernels"},
             "roofline": roofline, "clocks": clk, "gpu_launches": 2 * a.steps}
     if world == 1 and not a.no_extras:
         line["workloads"] = run_extras(G, flush, stream)

@@ -200,6 +200,12 @@ class Simulator:
             float(c), d_out.data_ptr(), ctypes.c_void_p(stream)), "gpurir_simulate_rir_device")
         return d_out
 
+    def last_output_direct(self):
+        """True when the last host-buffer call stored its RIRs from the kernels (no copy)."""
+        v = ctypes.c_int()
+        _lib.check(self._L.gpurir_last_output_direct(self._h, ctypes.byref(v)), "last_output_direct")
+        return bool(v.value)
+
     def set_profiling(self, on=True):
         _lib.check(self._L.gpurir_set_profiling(self._h, int(bool(on))), "set_profiling")
 

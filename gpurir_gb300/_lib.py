@@ -45,6 +45,7 @@ SIGNATURES = {
     "gpurir_set_profiling": (c_int, [c_void_p, c_int]),
     "gpurir_last_timing": (c_int, [c_void_p, fptr, fptr]),
     "gpurir_last_transfer_bytes": (c_int, [c_void_p, u64ptr, u64ptr]),
+    "gpurir_last_output_direct": (c_int, [c_void_p, iptr]),
     "gpurir_probe_peaks": (c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 

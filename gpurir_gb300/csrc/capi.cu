@@ -8,6 +8,8 @@
 // two kernels run back to back on one stream, and errors come back as codes.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -25,7 +27,7 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw);
+                               int tw, const TailArgs *tail);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
@@ -92,6 +94,8 @@ struct gpurir_sim {
     long last_n_rir = 0;
     size_t env_off = 0;        // offset of the envelope array in d_ws
     int profile = 0;           // record events around each kernel
+    int host_direct = -1;      // kernels may store into pageable host memory (-1: not yet queried)
+    bool last_direct = false;  // the last host call wrote its RIRs from the kernels
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_ism = false, ev_tail = false;
     uint64_t last_h2d = 0, last_d2h = 0;
@@ -314,6 +318,7 @@ static int ensure_stage(gpurir_sim *s, size_t bytes) {
 
 struct Plan {
     int tpl, em, nsub, grid, clamp;
+    long unfused_tails = 0;   // RIRs whose tail the separate tail kernel writes
     int mode = 0, tw = 0;   // tap evaluation mode (0 FP32, 1 mixed precision, 2 LUT), window length
     int max_n_diff;
     std::vector<IsmItem> items;
@@ -356,6 +361,7 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     }
     P.items.clear();
     P.rirs.clear();
+    P.unfused_tails = 0;
     P.rirs.reserve(M_tot);
     const long seg_max = std::min<long>((long)max_nsub * sub, 16384);   // int16 image offsets
     const long target = 4L * s->num_sms;
@@ -374,6 +380,8 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
             n_seg = (r.n_ism + tseg - 1) / tseg;
             P.nsub = std::max<int>(P.nsub, (int)((tseg + sub - 1) / sub));
         }
+        // a single-segment RIR gets its tail from the ISM kernel's epilogue
+        const bool fused = n_seg == 1 && r.n_total > r.n_ism;
         for (long m = 0; m < M; m++) {
             IsmItem it{};
             it.room = (int)ri;
@@ -381,7 +389,10 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
             it.rcv = r.rcv_off + (int)(m % r.n_rcv);
             it.rir = r.rir_off + (int)m;
             it.out_row = r.out_off + (long long)m * r.n_total;
-            P.rirs.push_back(it);
+            IsmItem ref = it;
+            ref.t_hi = fused ? -1 : 0;   // -1: the tail kernel skips this RIR
+            P.rirs.push_back(ref);
+            if (!fused && r.n_total > r.n_ism) P.unfused_tails++;
             for (long g = 0; g < n_seg; g++) {
                 IsmItem w = it;
                 w.t_lo = (int)(g * tseg);
@@ -451,18 +462,51 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
                            cudaStream_t st, bool record) {
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + L.o_rooms);
     if (record && s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
+    TailArgs ta;
+    ta.seed = s->seed;
+    ta.offset = s->calls;
+    ta.offset_ptr = offset_ptr;
+    ta.noise_kind = s->noise;
+    ta.env_out = reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env);
+    ta.fuse = 1;
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
-                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw));
+                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw, &ta));
     if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
-    if (record && s->profile && P.max_n_diff > 0) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
-    if (P.max_n_diff > 0)
+    const bool tail_kernel = P.max_n_diff > 0 && (P.unfused_tails > 0 || P.grid == 0);
+    if (record && s->profile && tail_kernel) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
+    if (tail_kernel)
         CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_rirs), (int)M, P.max_n_diff,
                        dps, dpr, dout, s->seed, s->calls, offset_ptr, s->noise,
                        reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env), st));
     if (record && s->ev_tail) CK(cudaEventRecord(s->ev[3], st));
     return GPURIR_OK;
+}
+
+// Device-usable address of a host output buffer, or nullptr when the kernels
+// cannot store to it (then the result is copied).  Pinned / registered memory
+// has a mapped device address; ordinary pageable memory is usable when the
+// device accesses it through the host page tables (address translation
+// services).  GPURIR_HOST_DIRECT=0 in the environment turns this off.
+static float *host_output_pointer(gpurir_sim *s, float *out) {
+    if (s->host_direct < 0) {
+        const char *env = getenv("GPURIR_HOST_DIRECT");
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, s->device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, s->device);
+        s->host_direct = (env && env[0] == '0') ? 0 : (pageable && host_tables ? 2 : 1);
+        cudaGetLastError();
+    }
+    if (s->host_direct == 0) return nullptr;
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, out) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (pa.type == cudaMemoryTypeHost && pa.devicePointer) return static_cast<float *>(pa.devicePointer);
+    if (pa.type == cudaMemoryTypeUnregistered && s->host_direct == 2) return out;
+    return nullptr;
 }
 
 // Shared body of the single-room and batched entry points, host or device I/O.
@@ -498,6 +542,15 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     CK(cudaEventRecord(s->stage_done, st));
     s->stage_pending = true;
     float *dout = host_io ? reinterpret_cast<float *>(d + L.o_out) : out;
+    // Host output the GPU can store to directly (pinned memory, or any host memory on
+    // systems whose GPU shares the CPU's page tables, e.g. over NVLink-C2C): the kernels
+    // write the RIRs there during compute and no device->host copy follows.
+    bool direct = false;
+    if (host_io) {
+        float *hp = host_output_pointer(s, out);
+        if (hp) { dout = hp; direct = true; }
+    }
+    s->last_direct = direct;
     s->ev_ism = s->ev_tail = false;
     s->last_h2d = L.stage_bytes;
     s->last_d2h = sizeof(int) + (host_io ? (uint64_t)out_elems * sizeof(float) : 0);
@@ -507,7 +560,7 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     s->last_n_rir = P.max_n_diff > 0 ? M : 0;
     s->calls++;
     CK(cudaMemcpyAsync(s->h_ctl + 1, s->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    if (host_io)
+    if (host_io && !direct)
         CK(cudaMemcpyAsync(out, dout, (size_t)out_elems * sizeof(float), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(s->ws_busy, st));
     s->ws_recorded = true;
@@ -1093,3 +1146,9 @@ int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub) {
 
 int set_last_error(int code, const char *msg) { return fail(code, msg); }
 }  // namespace gpurir
+
+extern "C" int gpurir_last_output_direct(gpurir_sim *s, int *direct) {
+    if (!s || !direct) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *direct = s->last_direct ? 1 : 0;
+    return GPURIR_OK;
+}

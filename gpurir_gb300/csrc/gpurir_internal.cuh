@@ -138,6 +138,16 @@ __device__ __forceinline__ float u01(uint32_t x) {
     return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f;
 }
 
+// Diffuse-tail parameters passed to the ISM kernel, whose epilogue writes the
+// tail of every RIR that is a single work item.
+struct TailArgs {
+    uint64_t seed, offset;
+    const uint64_t *offset_ptr;   // if set, the call offset is read there (captured graphs)
+    int noise_kind;
+    float *env_out;               // optional [rir][3]: A, alpha, tau_dp
+    int fuse;
+};
+
 // Error codes shared by kernels and host (written to a device status word).
 enum DevError : int { DEV_OK = 0, DEV_BAD_ITEM = 1, DEV_BAD_ROOM = 2 };
 

@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 
 #include "gpurir_internal.cuh"
+#include "tail_common.cuh"
 
 namespace gpurir {
 
@@ -36,6 +37,7 @@ constexpr int kRounds = kPerWarp / 32;              // 32-image rounds per warp 
 constexpr int kMaxSub = 64;                         // sub-ranges per item
 constexpr int kPool = kWarps;                       // extra slices of heavy sub-ranges per chunk
 constexpr int kMaxItems = 128;                      // >= kMaxSub + kPool queue entries
+static_assert(kThreads == kPowerThreads, "the fused tail sums the window power in the tail kernel's order");
 
 struct IsmLaunch {
     const RoomDesc *rooms;
@@ -50,6 +52,12 @@ struct IsmLaunch {
     int max_nsub;                     // sub-ranges this launch's smem holds
     int clamp;                        // taps may fall outside |x| < H: clamp the window
     int tw;                           // window length in samples (LUT mode table)
+    // diffuse tail written by the epilogue of single-segment items (see TailArgs)
+    uint64_t seed, offset;
+    const uint64_t *offset_ptr;
+    int noise_kind;
+    float *env_out;
+    int fuse_tail;
 };
 
 // Evaluation modes of the taps (template parameter MODE):
@@ -462,8 +470,18 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             }
             __syncthreads();
         }
-        // ---- output: sum of the covering sub-range buffers, ascending s
+        // ---- output: sum of the covering sub-range buffers, ascending s.  An item that
+        //      holds a whole early part also predicts the envelope from it and writes the
+        //      diffuse tail, so those stores overlap other blocks' tap work.
         float *orow = P.out + it.out_row;
+        const bool fuse = P.fuse_tail && t_lo == 0 && t_hi == R.n_ism && R.n_total > R.n_ism;
+        float tau_dp = 0.0f;
+        int w_start = t_hi;
+        if (fuse) {
+            tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
+            w_start = envelope_start(R, tau_dp);
+        }
+        float pw = 0.0f;
         for (int t = t_lo + tid; t < t_hi; t += kThreads) {
             const int rel = t - t_lo;
             int s_max = (rel - k_lo) / SUB;
@@ -473,6 +491,30 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             float acc = 0.0f;
             for (int s = s_min; s <= s_max; s++) acc += buf[P.em + s * BUF + rel - s * SUB - k_lo];
             orow[t] = acc;
+            if (t >= w_start) pw = fmaf(acc, acc, pw);
+        }
+        if (fuse) {
+            float *red = reinterpret_cast<float *>(hist);   // free until the next item
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) pw += __shfl_xor_sync(0xffffffffu, pw, o);
+            if (lane == 0) red[warp] = pw;
+            __syncthreads();
+            if (tid == 0) {
+                float tot = 0.0f;
+                for (int w = 0; w < kWarps; w++) tot += red[w];
+                const TailEnv e = tail_envelope(R, tot, w_start, tau_dp);
+                red[kWarps] = e.ea;
+                red[kWarps + 1] = e.eb;
+                if (P.env_out) {
+                    P.env_out[3 * it.rir] = e.A;
+                    P.env_out[3 * it.rir + 1] = e.alpha;
+                    P.env_out[3 * it.rir + 2] = tau_dp;
+                }
+            }
+            __syncthreads();
+            const uint64_t offset = P.offset_ptr ? *P.offset_ptr : P.offset;
+            tail_fill(orow + R.n_ism, R.n_total - R.n_ism, 0, R.n_total - R.n_ism, tid, kThreads,
+                      red[kWarps], red[kWarps + 1], P.seed, offset, (uint32_t)it.rir, P.noise_kind);
         }
         __syncthreads();
     }
@@ -560,8 +602,14 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw) {
+                               int tw, const TailArgs *tail) {
     IsmLaunch p;
+    p.seed = tail ? tail->seed : 0;
+    p.offset = tail ? tail->offset : 0;
+    p.offset_ptr = tail ? tail->offset_ptr : nullptr;
+    p.noise_kind = tail ? tail->noise_kind : 0;
+    p.env_out = tail ? tail->env_out : nullptr;
+    p.fuse_tail = tail ? tail->fuse : 0;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
     p.out = out; p.work_counter = work_counter; p.status = status;

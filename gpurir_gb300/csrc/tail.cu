@@ -7,11 +7,12 @@
 // Philox4x32-10 stream keyed by (seed, call offset, global RIR index), so the
 // noise is reproducible and needs no generator state or extra HBM pass.
 #include "gpurir_internal.cuh"
+#include "tail_common.cuh"
 
 namespace gpurir {
 
-constexpr int kTailThreads = 256;
-constexpr int kTailChunk = kTailThreads * 16;   // samples per block (4 Philox blocks/thread)
+constexpr int kTailThreads = kPowerThreads;
+constexpr int kTailChunk = kTailThreads * 8;   // samples per block (2 Philox blocks/thread)
 
 struct TailLaunch {
     const RoomDesc *rooms;
@@ -25,21 +26,11 @@ struct TailLaunch {
     float *env_out;          // optional [n_rir][3]: A, alpha, tau_dp
 };
 
-// Direct-path delay in samples, same float-float arithmetic as the ISM kernel
-// applies to the image with clust = refl = 0 (src/gpuRIR_cuda.cu:368-369).
-__device__ __forceinline__ float direct_tau(const RoomDesc &R, const float *ps, const float *pr) {
-    ff v0 = ff_two_sum(ps[0], -pr[0]);
-    ff v1 = ff_two_sum(ps[1], -pr[1]);
-    ff v2 = ff_two_sum(ps[2], -pr[2]);
-    ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
-    ff tau = ff_mul(ff_sqrt(d2), ff{R.kh, R.kl});
-    return tau.hi + tau.lo;
-}
-
 __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
     const int rir = blockIdx.x;
     if (rir >= P.n_rir) return;
     const IsmItem it = P.rirs[rir];
+    if (it.t_hi < 0) return;   // this RIR's tail was written by the ISM kernel's epilogue
     const RoomDesc &R = P.rooms[it.room];
     const int n_ism = R.n_ism, n_diff = R.n_total - R.n_ism;
     const int s0 = blockIdx.y * kTailChunk;
@@ -49,13 +40,10 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
     __shared__ float red[kTailThreads / 32];
     __shared__ float envA, envB;
     const float tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
-    // envelope window, src/gpuRIR_cuda.cu:419-428
-    const float w_sz = 10e-3f * R.fs;
-    const float lo = fmaxf((float)n_ism - w_sz, tau_dp);
-    const int w_start = (int)ceilf(lo);
-    const int cnt = n_ism - w_start;
+    const int w_start = envelope_start(R, tau_dp);
     float p = 0.0f;
-    for (int t = w_start + threadIdx.x; t < n_ism; t += kTailThreads) {
+    for (int t = (w_start / kTailThreads) * kTailThreads + threadIdx.x; t < n_ism; t += kTailThreads) {
+        if (t < w_start) continue;
         float v = row[t];
         p = fmaf(v, v, p);
     }
@@ -66,55 +54,19 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
     if (threadIdx.x == 0) {
         float tot = 0.0f;
         for (int w = 0; w < kTailThreads / 32; w++) tot += red[w];
-        const float alpha = -13.8155f / (R.T60 * R.fs);   // log(1e-6) / (T60 Fs)
-        float A = 0.0f;
-        if (cnt > 0) {
-            const float w_center = (float)w_start + (float)cnt * 0.5f;
-            A = (tot / (float)cnt) / expf(alpha * (w_center - tau_dp));
-        }
-        // out = sqrt(A exp(alpha (n_ism + s - tau_dp))) * noise = exp(B + 0.5 alpha s) * noise
-        envA = 0.5f * alpha;
-        envB = (A > 0.0f) ? 0.5f * logf(A) + 0.5f * alpha * ((float)n_ism - tau_dp) : -INFINITY;
+        const TailEnv e = tail_envelope(R, tot, w_start, tau_dp);
+        envA = e.ea;
+        envB = e.eb;
         if (P.env_out && blockIdx.y == 0) {
-            P.env_out[3 * rir] = A;
-            P.env_out[3 * rir + 1] = alpha;
+            P.env_out[3 * rir] = e.A;
+            P.env_out[3 * rir + 1] = e.alpha;
             P.env_out[3 * rir + 2] = tau_dp;
         }
     }
     __syncthreads();
-    const float ea = envA, eb = envB;
-    const uint2 key = make_uint2((uint32_t)P.seed, (uint32_t)(P.seed >> 32));
     const uint64_t offset = P.offset_ptr ? *P.offset_ptr : P.offset;
-    const uint32_t off_lo = (uint32_t)offset, off_hi = (uint32_t)(offset >> 32);
-    const uint32_t gidx = (uint32_t)it.rir;
-    float *trow = row + n_ism;
-#pragma unroll 1
-    for (int q = 0; q < kTailChunk / (4 * kTailThreads); q++) {
-        const int s = s0 + 4 * (q * kTailThreads + threadIdx.x);
-        if (s >= n_diff) break;
-        const uint4 w = philox4x32_10(make_uint4((uint32_t)(s >> 2), gidx, off_lo, off_hi), key);
-        float z[4];
-        if (P.noise_kind == 0) {
-            // logistic noise of unit variance, src/gpuRIR_cuda.cu:454-455
-            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const float u = u01(ww[e]);
-                z[e] = 0.551329f * __logf(u / (1.0f - u + 1e-6f));
-            }
-        } else {
-            const float r0 = sqrtf(-2.0f * __logf(u01(w.x)));
-            const float r1 = sqrtf(-2.0f * __logf(u01(w.z)));
-            float sn0, cs0, sn1, cs1;
-            sincospif(2.0f * u01(w.y), &sn0, &cs0);
-            sincospif(2.0f * u01(w.w), &sn1, &cs1);
-            z[0] = r0 * cs0; z[1] = r0 * sn0; z[2] = r1 * cs1; z[3] = r1 * sn1;
-        }
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            if (s + e < n_diff) trow[s + e] = __expf(fmaf(ea, (float)(s + e), eb)) * z[e];
-        }
-    }
+    tail_fill(row + n_ism, n_diff, s0, s0 + kTailChunk, threadIdx.x, kTailThreads, envA, envB, P.seed,
+              offset, (uint32_t)it.rir, P.noise_kind);
 }
 
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,

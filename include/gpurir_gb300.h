@@ -212,6 +212,13 @@ int gpurir_philox_stream_device(uint64_t seed, uint64_t call_counter, uint32_t r
  * as the tail used them (src/gpuRIR_cuda.cu:415-443).  `out` holds 3*n floats. */
 int gpurir_last_envelope(gpurir_sim *sim, float *out, long n);
 
+/* Whether the last gpurir_simulate_rir call stored the RIRs into the caller's
+ * host buffer from the kernels (1: pinned memory, or pageable memory on a GPU
+ * that uses the host page tables, such as GB300 over NVLink-C2C) or copied them
+ * after the kernels (0).  Setting GPURIR_HOST_DIRECT=0 in the environment forces
+ * the copy.  No counterpart in the reference. */
+int gpurir_last_output_direct(gpurir_sim *sim, int *direct);
+
 /* Kernel timing: when on, each simulate call records CUDA events on its
  * stream around the ISM kernel and the tail kernel; gpurir_last_timing waits
  * for them and returns the two durations in ms (0 for a kernel not launched).
