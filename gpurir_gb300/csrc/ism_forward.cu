@@ -66,8 +66,9 @@ struct IsmLaunch {
 //             and accumulation in FP32 (gpuRIR's activateMixedPrecision,
 //             src/gpuRIR_cuda.cu:488-553 evaluates in half2 and also accumulates in half2)
 //   kModeLUT  gpuRIR's lookup table (src/gpuRIR_cuda.cu:236-239, 578-616): Hann x sinc
-//             sampled 16x per sample, linear interpolation with an 8-bit fractional
-//             weight as texture filtering applies it, support |x| < floor(Tw/2)
+//             sampled 16x per sample, fetched at gpuRIR's float coordinate with the
+//             linear filter of a GB300 texture unit (8-bit weight, rounded half up),
+//             support |x| < floor(Tw/2)
 constexpr int kModeF32 = 0, kModeMP = 1, kModeLUT = 2;
 constexpr int kLutOversamp = 16;
 
@@ -113,19 +114,25 @@ __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], c
             p[32 * (i + 1)] = fmaf(al, v1, p[32 * (i + 1)]);
         }
     } else {
-        // record: al = amp, r.z = 8-bit weight, r.w = table index of tap k = 0
-        const float alpha = r.z;
-        const int base = __float_as_int(r.w);
-        const float2 *row = lut + (base & (kLutOversamp - 1)) * lut_cols;
-        const int col0 = base >> 4;
+        // gpuRIR's fetch (image_sample_lut, src/gpuRIR_cuda.cu:236-239) in its float
+        // arithmetic: record al = amp, r.y = f with tau = n0 + f exactly in float32, so
+        // x = k - f rounds as the reference's t - tau does; texel position
+        // __fmaf_rz(x, 16, 8 Tw + 0.5) - 0.5; the upper texel's weight on 8 fractional
+        // bits rounded half up, as GB300 texture units filter; border texels are 0.
+        const float lut_c = (float)(kLutOversamp / 2 * (lut_cols - 1)) + 0.5f;
+        const int j_max = kLutOversamp * (lut_cols - 1);
 #pragma unroll
         for (int i = 0; i < TPL; i++) {
             const float x = kf[i] - f;
-            int col = col0 + (int)kf[i];
-            const bool in = fabsf(x) < H && col >= 0 && col < lut_cols;
-            col = min(max(col, 0), lut_cols - 1);
-            const float2 t = row[col];
-            const float v = in ? fmaf(alpha, t.y - t.x, t.x) : 0.0f;
+            const float xb = __fmaf_rz(x, (float)kLutOversamp, lut_c) - 0.5f;
+            const float jf = floorf(xb);
+            const float y = (xb - jf) * 256.0f;   // exact
+            const float q = floorf(y);
+            const float w = (q + (y - q >= 0.5f ? 1.0f : 0.0f)) * (1.0f / 256.0f);
+            const int j = min(max((int)jf, 0), j_max);
+            const float2 t = lut[(j & (kLutOversamp - 1)) * lut_cols + (j >> 4)];
+            float v = fmaf(w, t.y - t.x, t.x);
+            v = fabsf(x) < H ? v : 0.0f;
             p[32 * i] = fmaf(al, v, p[32 * i]);
         }
     }
@@ -309,16 +316,11 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
                     f = fmaxf(f, 9.094947017729282e-13f);   // 2^-40: keeps x = k - f != 0
                     if (MODE == kModeLUT) {
-                        // texture coordinate of tap k: 16 (k - f) + 8 Tw; weight on 8 fractional
-                        // bits.  16 f and its fractional part are exact in float32, so the weight
-                        // is quantised from an exact fraction (forming 8 Tw - 16 f first would not be).
-                        const float g = 16.0f * f, gi = floorf(g), gf = g - gi;
-                        int base = 8 * P.tw - (int)gi - (gf > 0.0f ? 1 : 0);
-                        float alpha = gf > 0.0f ? rintf((1.0f - gf) * 256.0f) * (1.0f / 256.0f) : 0.0f;
-                        if (alpha >= 1.0f) { base += 1; alpha = 0.0f; }
+                        // the reference stores tau as a float: split its nearest float
+                        fl = floorf(tau.hi);
+                        n0 = (int)fl;
+                        f = tau.hi - fl;   // exact
                         a = amp;
-                        cphi = alpha;
-                        sphi = __int_as_float(base);
                     } else {
                         a = -amp * sinpif(f) * 0.318309886183790672f;
                         sincospif(f * inv_h, &sphi, &cphi);   // phi = 2 pi f / Tw

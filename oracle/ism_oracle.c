@@ -9,11 +9,12 @@
  *   - The host-side helpers and the trajectory overlap-add it is used with are
  *     pinned against golden vectors produced by importing the reference's own
  *     Python package (tests/golden/make_golden.py).
- *   - The CUDA kernels of the reference (src/gpuRIR_cuda.cu) cannot be executed
- *     in the build container (no GPU) nor on the GPU host (the reference sources
- *     are not present there), so the ISM arithmetic below is PARITY UNPINNED
- *     against a run of the reference; it is a line-by-line restatement of the
- *     formulas cited below, checked by hand-derived known answers in tests/.
+ *   - The ISM arithmetic is pinned against the reference's own CUDA kernels:
+ *     src/gpuRIR_cuda.cu compiled from the reference sources (oracle/ref_kernels.py)
+ *     and run on a GB300 produced tests/golden/reference_kernels.npz.  Fed the
+ *     reference's image amplitudes and delays, orc_ism_sum, orc_ism_sum_lut,
+ *     orc_env_pred and orc_diffuse_from_uniforms reproduce those kernels to
+ *     float32 rounding (tests/test_reference_kernels.py).
  *
  * Every function names the reference lines (path:line inside the gpuRIR
  * project) that it restates.  Arithmetic is FP64 unless the name says f32.
@@ -164,21 +165,15 @@ void orc_ism_sum(const double *amp, const double *tau, long M, long N, int nISM,
     }
 }
 
-/*
- * Lookup-table variant of the early part, restating gpuRIR's LUT path:
- * the table of create_sinc_texture_lut (src/gpuRIR_cuda.cu:578-592: Hann x sinc
- * at 16 samples per sample, lut_len = 16 Tw + 1, float arithmetic), the fetch
- * coordinate of image_sample_lut (:236-239: 16 (t - tau) + lut_len/2 + 0.5,
- * support |t - tau| < Tw/2 in integer division) and linear texture filtering
- * with the weight held on 8 fractional bits (rounded to nearest here).
- */
-void orc_ism_sum_lut(const double *amp, const double *tau, long M, long N, int nISM, float Fs,
-                     double *rir, long ld)
+int orc_lut_len(float Fs) { return orc_window_len(Fs) * 16 + 1; }
+
+/* The Hann x sinc table of create_sinc_texture_lut (src/gpuRIR_cuda.cu:578-592),
+ * float arithmetic, symmetric about lut_len/2: T[lut_len/2 +- i] at x = i/16. */
+void orc_lut_table(float Fs, float *T)
 {
     const int Tw = orc_window_len(Fs);
-    const int lut_len = Tw * 16 + 1, center = lut_len / 2, H = Tw / 2;
+    const int lut_len = orc_lut_len(Fs), center = lut_len / 2;
     const float PIf = 3.141592654f;
-    float *T = (float *)malloc(sizeof(float) * (size_t)(lut_len + 1));
     for (int i = 0; i <= center; i++) {
         float x = (float)i / 16;
         float sc = (x == 0.0f) ? 1.0f : sinf(PIf * x) / (PIf * x);
@@ -186,20 +181,57 @@ void orc_ism_sum_lut(const double *amp, const double *tau, long M, long N, int n
         T[center + i] = hn * sc;
         T[center - i] = hn * sc;
     }
+}
+
+/* fmaf(a, b, c) rounded toward zero (the __fmaf_rz of image_sample_lut) for a
+ * result > 0: the exact value is s + e (TwoSum of a*b, exact in double, and c),
+ * and the nearest float is stepped down when it lies above it. */
+static float orc_fmaf_rz_pos(float a, float b, float c)
+{
+    const double p = (double)a * (double)b, q = (double)c;
+    const double s = p + q;
+    const double bb = s - p;
+    const double e = (p - (s - bb)) + (q - bb);
+    float f = (float)s;
+    if ((double)f - s > e) f = nextafterf(f, 0.0f);
+    return f;
+}
+
+/*
+ * Lookup-table variant of the early part, restating gpuRIR's LUT path in its
+ * float arithmetic: the table of create_sinc_texture_lut (src/gpuRIR_cuda.cu:
+ * 578-592: Hann x sinc at 16 samples per sample, lut_len = 16 Tw + 1), the fetch
+ * of image_sample_lut (:236-239): t_tau = t - tau in float, support
+ * |t_tau| < Tw/2 (integer division), coordinate __fmaf_rz(t_tau, 16,
+ * lut_len/2 + 0.5), and the linear filter of a float texture: texel position
+ * x - 0.5, weight of the upper texel held on 8 fractional bits, rounded half up
+ * (measured on GB300 texture units), border texels 0.  tau is taken as the
+ * nearest float, as the reference stores it.
+ */
+void orc_ism_sum_lut(const double *amp, const double *tau, long M, long N, int nISM, float Fs,
+                     double *rir, long ld)
+{
+    const int Tw = orc_window_len(Fs);
+    const int lut_len = orc_lut_len(Fs), center = lut_len / 2, H = Tw / 2;
+    const float cfetch = (float)center + 0.5f;
+    float *T = (float *)malloc(sizeof(float) * (size_t)(lut_len + 1));
+    orc_lut_table(Fs, T);
     T[lut_len] = 0.0f;
     for (long m = 0; m < M; m++) {
         double *h = rir + m * ld;
         for (int t = 0; t < nISM; t++) h[t] = 0.0;
         for (long i = 0; i < N; i++) {
-            double a = amp[m * N + i], ta = tau[m * N + i];
-            long t0 = (long)floor(ta - H);
+            const double a = amp[m * N + i];
+            const float tf = (float)tau[m * N + i];
+            long t0 = (long)floor((double)tf - H) - 1;
             if (t0 < 0) t0 = 0;
-            for (long t = t0; t < nISM && (double)t < ta + H; t++) {
-                double x = (double)t - ta;
-                if (fabs(x) >= H) continue;
-                double xb = 16.0 * x + center;
-                long j = (long)floor(xb);
-                double al = nearbyint((xb - (double)j) * 256.0) / 256.0;
+            for (long t = t0; t < nISM && (double)t < (double)tf + H + 1; t++) {
+                const float x = (float)t - tf;
+                if (fabsf(x) >= (float)H) continue;
+                const float xb = orc_fmaf_rz_pos(x, 16.0f, cfetch) - 0.5f;
+                const float jf = floorf(xb);
+                long j = (long)jf;
+                double al = floor((double)(xb - jf) * 256.0 + 0.5) / 256.0;
                 if (al >= 1.0) { j += 1; al = 0.0; }
                 double t0v = (j >= 0 && j < lut_len) ? T[j] : 0.0;
                 double t1v = (j + 1 >= 0 && j + 1 < lut_len) ? T[j + 1] : 0.0;
@@ -291,6 +323,12 @@ void orc_tail_stream(uint64_t seed, uint64_t offset, uint32_t rir_index, long n,
  * value that float32 represents exactly. */
 static double orc_u01(uint32_t x) { return ((double)(x >> 9) + 0.5) * (1.0 / 8388608.0); }
 
+/* Tail sample s: noise z shaped by sqrt(A*exp(alpha*(nISM + s - tau_dp))) (:457-459). */
+static double orc_tail_sample(double A, double alpha, double tau_dp, int nISM, int s, double z)
+{
+    return sqrt(A * exp(alpha * ((double)nISM + s - tau_dp))) * z;
+}
+
 /*
  * Diffuse tail, restating diffRev_kernel (src/gpuRIR_cuda.cu:445-461): unit
  * variance noise shaped by sqrt(A*exp(alpha*(nISM + s - tau_dp))).
@@ -317,11 +355,23 @@ void orc_tail(const double *A, const double *alpha, const double *tau_dp, long M
                 double r = sqrt(-2.0 * log(u1));
                 z = (s & 1) ? r * sin(2.0 * ORC_PI * u2) : r * cos(2.0 * ORC_PI * u2);
             }
-            double env = A[m] * exp(alpha[m] * ((double)nISM + s - tau_dp[m]));
-            out[m * ld + nISM + s] = sqrt(env) * z;
+            out[m * ld + nISM + s] = orc_tail_sample(A[m], alpha[m], tau_dp[m], nISM, s, z);
         }
     }
     free(w);
+}
+
+/* diffRev_kernel (src/gpuRIR_cuda.cu:445-461) applied to given uniforms, as the
+ * reference applies it to the uniforms cuRAND wrote: u [M][nDiff] -> out [M][nDiff]. */
+void orc_diffuse_from_uniforms(const double *A, const double *alpha, const double *tau_dp, long M,
+                               int nISM, int nDiff, const float *u, double *out)
+{
+    for (long m = 0; m < M; m++)
+        for (int s = 0; s < nDiff; s++) {
+            const double v = u[m * nDiff + s];
+            const double z = 0.551329 * log(v / (1.0 - v + 1e-6));
+            out[m * nDiff + s] = orc_tail_sample(A[m], alpha[m], tau_dp[m], nISM, s, z);
+        }
 }
 
 /* ---------------------------------------------------------------------------

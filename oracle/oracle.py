@@ -56,6 +56,10 @@ def lib():
             L.orc_ism_sum.restype = None
             L.orc_ism_sum_lut.argtypes = L.orc_ism_sum.argtypes
             L.orc_ism_sum_lut.restype = None
+            L.orc_lut_len.argtypes = [ctypes.c_float]
+            L.orc_lut_len.restype = ctypes.c_int
+            L.orc_lut_table.argtypes = [ctypes.c_float, fp]
+            L.orc_lut_table.restype = None
             L.orc_sabine_t60.argtypes = [fp, fp]
             L.orc_sabine_t60.restype = ctypes.c_double
             L.orc_env_pred.argtypes = [dp, ctypes.c_long, dp, ctypes.c_long, ctypes.c_int,
@@ -70,6 +74,9 @@ def lib():
                                    ctypes.c_uint64, ctypes.c_uint64, up, ctypes.c_int, dp,
                                    ctypes.c_long]
             L.orc_tail.restype = None
+            L.orc_diffuse_from_uniforms.argtypes = [dp, dp, dp, ctypes.c_long, ctypes.c_int,
+                                                    ctypes.c_int, fp, dp]
+            L.orc_diffuse_from_uniforms.restype = None
             L.orc_ism_f32.argtypes = [fp, fp, fp, ctypes.c_int, fp, ctypes.c_int, fp, fp,
                                       ctypes.c_int, ctypes.c_int, ip, ctypes.c_float,
                                       ctypes.c_float, ctypes.c_int, fp, ctypes.c_long,
@@ -153,6 +160,14 @@ def ism_sum_lut(amp, tau, n_ism, fs, ld=None):
     return out
 
 
+def lut_table(fs):
+    """gpuRIR's Hann x sinc lookup table (float32, 16 Tw + 1 entries)."""
+    n = lib().orc_lut_len(float(np.float32(fs)))
+    T = np.zeros(n, dtype=np.float32)
+    lib().orc_lut_table(float(np.float32(fs)), _p(T, ctypes.c_float))
+    return T
+
+
 def sabine_t60(room_sz, beta):
     room = _f32(room_sz, (3,))
     b = _f32(beta, (6,))
@@ -185,6 +200,20 @@ def tail_stream(seed, offset, rir_index, n):
     o = np.zeros(int(n), dtype=np.uint32)
     lib().orc_tail_stream(int(seed), int(offset), int(rir_index), int(n), _p(o, ctypes.c_uint32))
     return o
+
+
+def diffuse_from_uniforms(A, alpha, tau_dp, n_ism, uniforms):
+    """The reference's tail transform applied to given uniforms: [M, nDiff] float64."""
+    A = np.ascontiguousarray(A, dtype=np.float64).ravel()
+    al = np.ascontiguousarray(alpha, dtype=np.float64).ravel()
+    tdp = np.ascontiguousarray(tau_dp, dtype=np.float64).ravel()
+    M = A.size
+    u = np.ascontiguousarray(uniforms, dtype=np.float32).reshape(M, -1)
+    out = np.zeros(u.shape)
+    lib().orc_diffuse_from_uniforms(_p(A, ctypes.c_double), _p(al, ctypes.c_double),
+                                    _p(tdp, ctypes.c_double), M, int(n_ism), u.shape[1],
+                                    _p(u, ctypes.c_float), _p(out, ctypes.c_double))
+    return out
 
 
 NOISE_KINDS = {"logistic": 0, "gaussian": 1}
