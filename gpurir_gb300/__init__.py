@@ -20,7 +20,7 @@ import ctypes
 
 import numpy as np
 
-from . import _lib
+from . import _hostmem, _lib
 from ._lib import GpuRirError
 
 __all__ = ["polar_patterns", "beta_SabineEstimation", "att2t_SabineEstimator", "t2n",
@@ -169,7 +169,8 @@ class Simulator:
             raise ValueError("orientations must have the shape of the positions")
         ns = self._L.gpurir_n_samples(float(Tmax), float(fs))
         if out is None:
-            out = np.empty((ms, mr, ns), dtype=np.float32)
+            # page-locked and reused across calls: the kernels store into it directly
+            out = _hostmem.pool().empty((ms, mr, ns), np.float32)
         assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == (ms, mr, ns)
         _lib.check(self._L.gpurir_simulate_rir(
             self._h, room.ctypes.data_as(_lib.fptr), b.ctypes.data_as(_lib.fptr),

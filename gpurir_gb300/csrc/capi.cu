@@ -485,17 +485,19 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
 }
 
 // Device-usable address of a host output buffer, or nullptr when the kernels
-// cannot store to it (then the result is copied).  Pinned / registered memory
-// has a mapped device address; ordinary pageable memory is usable when the
-// device accesses it through the host page tables (address translation
-// services).  GPURIR_HOST_DIRECT=0 in the environment turns this off.
+// do not store to it (then the result is copied).  Pinned / registered memory
+// has a mapped device address.  Pageable memory is copied into by default: a
+// GPU that reads the host page tables (address translation services) can
+// store into it, but pages not yet touched fault one by one from the GPU side,
+// far slower than the copy.  GPURIR_HOST_DIRECT=0 turns direct stores off,
+// =2 allows them into pageable memory as well.
 static float *host_output_pointer(gpurir_sim *s, float *out) {
     if (s->host_direct < 0) {
         const char *env = getenv("GPURIR_HOST_DIRECT");
         int pageable = 0, host_tables = 0;
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, s->device);
         cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, s->device);
-        s->host_direct = (env && env[0] == '0') ? 0 : (pageable && host_tables ? 2 : 1);
+        s->host_direct = (env && env[0] == '0') ? 0 : ((env && env[0] == '2' && pageable && host_tables) ? 2 : 1);
         cudaGetLastError();
     }
     if (s->host_direct == 0) return nullptr;
@@ -1146,6 +1148,29 @@ int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub) {
 
 int set_last_error(int code, const char *msg) { return fail(code, msg); }
 }  // namespace gpurir
+
+extern "C" int gpurir_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return fail(GPURIR_ERR_INVALID, "gpurir_host_alloc: ptr is NULL");
+    *ptr = nullptr;
+    if (bytes == 0) return GPURIR_OK;
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable | cudaHostAllocMapped);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        cudaGetLastError();
+        return fail(GPURIR_ERR_CUDA, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_host_free(void *ptr) {
+    if (!ptr) return GPURIR_OK;
+    cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GPURIR_ERR_CUDA, std::string("cudaFreeHost: ") + cudaGetErrorString(e));
+    }
+    return GPURIR_OK;
+}
 
 extern "C" int gpurir_last_output_direct(gpurir_sim *s, int *direct) {
     if (!s || !direct) return fail(GPURIR_ERR_INVALID, "NULL argument");

@@ -213,11 +213,21 @@ int gpurir_philox_stream_device(uint64_t seed, uint64_t call_counter, uint32_t r
 int gpurir_last_envelope(gpurir_sim *sim, float *out, long n);
 
 /* Whether the last gpurir_simulate_rir call stored the RIRs into the caller's
- * host buffer from the kernels (1: pinned memory, or pageable memory on a GPU
- * that uses the host page tables, such as GB300 over NVLink-C2C) or copied them
- * after the kernels (0).  Setting GPURIR_HOST_DIRECT=0 in the environment forces
- * the copy.  No counterpart in the reference. */
+ * host buffer from the kernels (1: page-locked memory, e.g. from
+ * gpurir_host_alloc) or copied them after the kernels (0: pageable memory).
+ * GPURIR_HOST_DIRECT=0 in the environment forces the copy; =2 also stores
+ * straight into pageable memory on a GPU that reads the host page tables
+ * (GB300 over NVLink-C2C), which is slow for pages never touched before.
+ * No counterpart in the reference. */
 int gpurir_last_output_direct(gpurir_sim *sim, int *direct);
+
+/* Page-locked, device-mapped host memory for result buffers (cudaHostAlloc):
+ * gpurir_simulate_rir stores into it from the kernels, overlapping the
+ * transfer with the computation.  No counterpart in the reference, which
+ * copies every result into a fresh pageable buffer (src/gpuRIR_cuda.cu:900-915,
+ * python_bind.cpp:77-86). */
+int gpurir_host_alloc(size_t bytes, void **ptr);
+int gpurir_host_free(void *ptr);
 
 /* Kernel timing: when on, each simulate call records CUDA events on its
  * stream around the ISM kernel and the tail kernel; gpurir_last_timing waits

@@ -260,10 +260,11 @@ class RefKernels:
     # -- cuda_simulateRIR, src/gpuRIR_cuda.cu:766-931 -----------------------------------
     def simulate(self, room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
                  spkr_pattern=0, mic_pattern=0, orV_src=None, orV_rcv=None, c=343.0, mode="fp32",
-                 uniforms=None):
+                 uniforms=None, host=True):
         """Early part, envelope and (with `uniforms`, [M_src, M_rcv, nSamples - nSamplesISM]
-        float32 in (0, 1)) the diffuse tail, by the reference's kernels.  `mode` is
-        "fp32", "mp" (activateMixedPrecision) or "lut" (activateLUT)."""
+        float32 in (0, 1), numpy or a CUDA tensor) the diffuse tail, by the reference's
+        kernels.  `mode` is "fp32", "mp" (activateMixedPrecision) or "lut" (activateLUT).
+        host=False returns the device tensors and copies nothing back."""
         P = ctypes.c_void_p
         I, F = ctypes.c_int, ctypes.c_float
         room = np.asarray(room_sz, dtype=np.float32).reshape(3)
@@ -301,18 +302,23 @@ class RefKernels:
                      [(P, A.data_ptr()), (P, alpha.data_ptr()), (P, rir.data_ptr()), (P, tau_dp.data_ptr()),
                       (I, ms), (I, mr), (I, n_ism), (F, float(np.float32(fs)))] +
                      [(F, float(v)) for v in room] + [(F, float(v)) for v in b])
-        out = dict(amp=amp.cpu().numpy().reshape(ms, mr, N), tau=tau.cpu().numpy().reshape(ms, mr, N),
-                   tau_dp=tau_dp.cpu().numpy().reshape(ms, mr), early=rir.cpu().numpy().reshape(ms, mr, n_ism),
-                   A=A.cpu().numpy().reshape(ms, mr), alpha=alpha.cpu().numpy().reshape(ms, mr),
-                   n_ism=n_ism, n_samples=n_tot)
+        out = dict(amp=amp, tau=tau, tau_dp=tau_dp, early=rir, A=A, alpha=alpha)
         if uniforms is not None and n_diff > 0:
-            u = np.ascontiguousarray(uniforms, dtype=np.float32).reshape(ms, mr, n_diff)
-            diff = self._dev(u)
+            if isinstance(uniforms, np.ndarray):
+                diff = self._dev(np.ascontiguousarray(uniforms, dtype=np.float32).reshape(-1))
+            else:
+                diff = uniforms.reshape(-1)
+            assert diff.numel() == M * n_diff and diff.dtype == self.torch.float32 and diff.is_cuda
             grid = (_ceil_f32(n_diff, _DIFF_BLOCK[0]), _ceil_f32(ms, _DIFF_BLOCK[1]), _ceil_f32(mr, _DIFF_BLOCK[2]))
             self._launch(K_DIFF, grid, _DIFF_BLOCK, 0,
                          [(P, diff.data_ptr()), (P, A.data_ptr()), (P, alpha.data_ptr()),
                           (P, tau_dp.data_ptr()), (I, ms), (I, mr), (I, n_ism), (I, n_diff)])
-            out["diffuse"] = diff.cpu().numpy().reshape(ms, mr, n_diff)
+            out["diffuse"] = diff
+        shapes = dict(amp=(ms, mr, N), tau=(ms, mr, N), tau_dp=(ms, mr), early=(ms, mr, n_ism),
+                      A=(ms, mr), alpha=(ms, mr), diffuse=(ms, mr, n_diff))
+        if host:
+            out = {k: v.cpu().numpy().reshape(shapes[k]) for k, v in out.items()}
+        out.update(n_ism=n_ism, n_samples=n_tot)
         return out
 
     def close(self):
