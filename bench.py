@@ -50,6 +50,8 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the batched / adjoint / trajectory measurements")
+    p.add_argument("--extras", default="batched,inverse,trajectory",
+                   help="comma list of the extra measurements to run (batched, inverse, trajectory)")
     return p.parse_args()
 
 
@@ -182,22 +184,34 @@ def _timed(fn, steps, stream, flush=None):
     return ts[len(ts) // 2]
 
 
-def run_extras(G, flush, stream):
+def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory")):
     """The metric's other parts: batched vs plain forward (512 uneven rooms), forward +
     adjoint step vs forward (16 rooms x 32 RIRs), trajectory filtering (400 points)."""
     import torch
     from gpurir_gb300 import batch as B, workloads
     out = {}
+    fs = 16000.0
+    dev = stream.device
+    sim = G.Simulator(seed=7)
+    if "batched" in which:
+        out.update(_extra_batched(G, B, workloads, sim, flush, stream, fs, dev))
+    if "inverse" in which:
+        out.update(_extra_inverse(workloads, sim, flush, stream, fs, dev))
+    if "trajectory" in which:
+        out.update(_extra_trajectory(workloads, sim, flush, stream, fs, dev))
+    return out
+
+
+def _extra_batched(G, B, workloads, sim, flush, stream, fs, dev):
+    import torch
+    out = {}
     # -- batched rooms: one captured launch vs one call per room
     rooms = workloads.batched_rooms()
-    fs = 16000.0
     n_rir = sum(r["pos_src"].shape[0] * r["pos_rcv"].shape[0] for r in rooms)
-    sim = G.Simulator(seed=7)
     plan = B.BatchPlan(rooms, fs, sim=sim)
     for _ in range(2):
         plan.launch(stream.cuda_stream)
     t_batch = _timed(lambda: plan.launch(stream.cuda_stream), 10, stream, flush)
-    dev = stream.device
     per_room = []
     for r in rooms:
         d = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
@@ -221,6 +235,12 @@ def run_extras(G, flush, stream):
         "batched_over_plain": t_plain / t_batch,
         "note": "batched = one CUDA-graph replay of all 512 rooms; plain = one device-API call "
                 "per room on the same stream"}
+    return out
+
+
+def _extra_inverse(workloads, sim, flush, stream, fs, dev):
+    import torch
+    out = {}
     # -- forward + adjoint step of the inverse problem
     from gpurir_gb300.autograd import simulate_batch_torch
     inv = workloads.inverse_problem()
@@ -247,6 +267,12 @@ def run_extras(G, flush, stream):
                               "adjoint_over_forward": t_fb / t_f,
                               "note": "grads of an L2 loss w.r.t. beta[16,6], pos_src[64,3], "
                                       "pos_rcv[128,3]; includes the host round trip of beta"}
+    return out
+
+
+def _extra_trajectory(workloads, sim, flush, stream, fs, dev):
+    import torch
+    out = {}
     # -- trajectory: RIRs simulated on the device, then convolution + overlap-add
     tr = workloads.trajectory()
     d = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
@@ -307,7 +333,7 @@ def run_gpu(a):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    total_ms, ism_ms, tail_ms = 0.0, [], []
+    total_ms, ism_ms, tail_ms, launches = 0.0, [], [], 0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for _ in range(a.steps):
         flush.zero_()
@@ -317,14 +343,14 @@ def run_gpu(a):
         ev1.synchronize()
         total_ms += ev0.elapsed_time(ev1)
         i_ms, t_ms = sim.last_timing()
+        launches += sim.last_launch_count()
         ism_ms.append(i_ms)
         tail_ms.append(t_ms)
     torch.cuda.synchronize()
     if world > 1:
+        from gpurir_gb300.replicas import max_over_ranks
         torch.distributed.barrier()
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms)
     clk = clocks.stop()
     ms_per_step = total_ms / a.steps
     value = world * M * a.steps / (total_ms * 1e-3)
@@ -349,9 +375,8 @@ def run_gpu(a):
     h2d, d2h = sim.last_transfer_bytes()
     direct = sim.last_output_direct()
     if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        from gpurir_gb300.replicas import max_over_ranks
+        e2e_s = max_over_ranks(e2e_s)
     e2e_value = world * M * a.steps / e2e_s
 
     if rank != 0:
@@ -372,7 +397,7 @@ def run_gpu(a):
         "unit": "Tops/s",
         "frac": frac_sfu if use_sfu else frac_fp32,
         "traffic": traffic,
-        "kernel": "ism_forward_kernel<4>",
+        "kernel": "ism_forward_kernel<4, 0> (diffuse tail fused into its epilogue)",
         "basis": "%d transcendental + %d FP32 ops per windowed image-sample update; %d updates "
                  "per launch; peaks measured on this device (MUFU rcp, FP32 FMA)" %
                  (SFU_PER_UPDATE, FLOPS_PER_UPDATE, updates),
@@ -393,9 +418,9 @@ def run_gpu(a):
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3,
                     "d2h": "kernel stores into the pinned host buffer over NVLink-C2C" if direct
                            else "cudaMemcpyAsync after the kernels"},
-            "roofline": roofline, "clocks": clk, "gpu_launches": 2 * a.steps}
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches}
     if world == 1 and not a.no_extras:
-        line["workloads"] = run_extras(G, flush, stream)
+        line["workloads"] = run_extras(G, flush, stream, tuple(a.extras.split(",")))
     if world == 1 and not a.no_cpu_baseline:
         scene_cpu = workloads.mic_array()
         threads = os.cpu_count() or 1

@@ -207,6 +207,12 @@ class Simulator:
         _lib.check(self._L.gpurir_last_output_direct(self._h, ctypes.byref(v)), "last_output_direct")
         return bool(v.value)
 
+    def last_launch_count(self):
+        """Kernels launched by the last simulate call (1 when the tail is fused)."""
+        v = ctypes.c_int()
+        _lib.check(self._L.gpurir_last_launch_count(self._h, ctypes.byref(v)), "last_launch_count")
+        return v.value
+
     def set_profiling(self, on=True):
         _lib.check(self._L.gpurir_set_profiling(self._h, int(bool(on))), "set_profiling")
 

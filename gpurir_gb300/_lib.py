@@ -46,6 +46,7 @@ SIGNATURES = {
     "gpurir_last_timing": (c_int, [c_void_p, fptr, fptr]),
     "gpurir_last_transfer_bytes": (c_int, [c_void_p, u64ptr, u64ptr]),
     "gpurir_last_output_direct": (c_int, [c_void_p, iptr]),
+    "gpurir_last_launch_count": (c_int, [c_void_p, iptr]),
     "gpurir_host_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
     "gpurir_host_free": (c_int, [c_void_p]),
     "gpurir_probe_peaks": (c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),

@@ -98,6 +98,7 @@ struct gpurir_sim {
     bool last_direct = false;  // the last host call wrote its RIRs from the kernels
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_ism = false, ev_tail = false;
+    int last_launches = 0;        // kernels the last simulate call launched
     uint64_t last_h2d = 0, last_d2h = 0;
     // convolution: twiddle tables per FFT size, and a grow-only workspace
     std::vector<std::pair<int, float2 *>> twiddles;
@@ -469,6 +470,7 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     ta.noise_kind = s->noise;
     ta.env_out = reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env);
     ta.fuse = 1;
+    if (record) s->last_launches = (P.grid > 0 ? 1 : 0);
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
@@ -476,6 +478,7 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
     const bool tail_kernel = P.max_n_diff > 0 && (P.unfused_tails > 0 || P.grid == 0);
     if (record && s->profile && tail_kernel) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }
+    if (record && tail_kernel) s->last_launches += 1;
     if (tail_kernel)
         CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_rirs), (int)M, P.max_n_diff,
                        dps, dpr, dout, s->seed, s->calls, offset_ptr, s->noise,
@@ -675,6 +678,12 @@ extern "C" int gpurir_set_profiling(gpurir_sim *s, int on) {
     if (on && !s->ev[0])
         for (int i = 0; i < 4; i++) CK(cudaEventCreate(&s->ev[i]));
     s->profile = on ? 1 : 0;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_last_launch_count(gpurir_sim *s, int *kernels) {
+    if (!s || !kernels) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *kernels = s->last_launches;
     return GPURIR_OK;
 }
 

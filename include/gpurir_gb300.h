@@ -229,6 +229,11 @@ int gpurir_last_output_direct(gpurir_sim *sim, int *direct);
 int gpurir_host_alloc(size_t bytes, void **ptr);
 int gpurir_host_free(void *ptr);
 
+/* Number of kernels the last simulate call on `sim` launched (ISM kernel, plus
+ * the tail kernel when some RIR spans several work items).  No counterpart in
+ * the reference. */
+int gpurir_last_launch_count(gpurir_sim *sim, int *kernels);
+
 /* Kernel timing: when on, each simulate call records CUDA events on its
  * stream around the ISM kernel and the tail kernel; gpurir_last_timing waits
  * for them and returns the two durations in ms (0 for a kernel not launched).
