@@ -12,6 +12,8 @@
 // in shared memory (M <= 8192) or in a per-block global scratch (larger M).
 // Twiddles come from a table W[m] = exp(-2 pi i m / N), m < N, built once per
 // size with sincospi.
+#include <algorithm>
+
 #include "gpurir_internal.cuh"
 
 namespace gpurir {
@@ -210,6 +212,247 @@ __global__ void __launch_bounds__(kFftThreads) rir_conv_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident FFT convolution for M = 1024 .. 8192 (N = 2M <= 16384).
+//
+// M/16 threads per row; each holds 16 complex values.  A Stockham pass of radix
+// 16 (then one of radix M/Ns in {2, 4, 8}) reads its 16 inputs from shared
+// memory, applies the twiddles, does the DFT in registers and writes its 16
+// outputs back: log16(M) + 1 round trips per FFT instead of log4(M) with two
+// buffers.  One buffer per row, padded by one element per 16 so that every
+// pass is free of bank conflicts; several rows per SM overlap their loads,
+// passes and stores.  The first pass reads the RIR straight from global memory.
+// ---------------------------------------------------------------------------
+constexpr float kC8 = 0.92387953251128674f;    // cos(pi/8)
+constexpr float kS8 = 0.38268343236508977f;    // sin(pi/8)
+constexpr float kR2 = 0.70710678118654752f;    // sqrt(2)/2
+
+__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+
+// x * (-i) (forward) or x * (+i) (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 rot_q(float2 a) {
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+// in place: a[0..3] -> X[0..3], X[k] = sum_n a[n] w4^(nk), w4 = exp(-+2 pi i/4)
+template <bool INV>
+__device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3) {
+    const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3);
+    const float2 t3 = rot_q<INV>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a1 = cadd(t1, t3);
+    a2 = csub(t0, t2);
+    a3 = csub(t1, t3);
+}
+
+// exp(-+2 pi i m/16) for the twiddles inside a radix-16 DFT
+template <bool INV>
+__device__ __forceinline__ float2 w16(int m) {
+    float c, s;
+    switch (m) {
+    case 1: c = kC8; s = kS8; break;
+    case 2: c = kR2; s = kR2; break;
+    case 3: c = kS8; s = kC8; break;
+    case 4: c = 0.0f; s = 1.0f; break;
+    case 6: c = -kR2; s = kR2; break;
+    case 9: c = -kC8; s = -kS8; break;
+    default: c = 1.0f; s = 0.0f; break;
+    }
+    return make_float2(c, INV ? s : -s);
+}
+
+// v[n], n = 4 n1 + n2  ->  V[k1 + 4 k2] held in v[4 k1 + k2] (digit-reversed; the
+// writer below reads output s from v[dr16(s)])
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+    // v[4 k1 + n2] now holds Y[k1][n2]; twiddle by w16^(n2 k1)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; k1++)
+#pragma unroll
+        for (int n2 = 1; n2 < 4; n2++) v[4 * k1 + n2] = cmul(v[4 * k1 + n2], w16<INV>(n2 * k1));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) dft4<INV>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+}
+
+__host__ __device__ constexpr int dr16(int s) { return 4 * (s & 3) + (s >> 2); }
+
+// One radix-16 Stockham pass at stride Ns for the thread's j (= thread index):
+// twiddle, DFT, write dst[(j - k) 16 + k + s Ns], k = j mod Ns.
+// W: exp(-2 pi i m/N) for m < N = 2M.
+template <bool INV, int M>
+__device__ __forceinline__ void pass16_compute_write(float2 (&v)[16], float2 *buf, int j, int Ns,
+                                                     const float2 *__restrict__ W) {
+    const int k = j & (Ns - 1);
+    if (Ns > 1) {
+        const int step = (2 * M) / (Ns * 16);   // W_{16 Ns}^1 = W_N^step
+#pragma unroll
+        for (int r = 1; r < 16; r++) {
+            float2 w = __ldg(&W[r * k * step]);
+            if (INV) w = cconj(w);
+            v[r] = cmul(v[r], w);
+        }
+    }
+    dft16<INV>(v);
+    const int base = (j - k) * 16 + k;
+#pragma unroll
+    for (int s = 0; s < 16; s++) buf[pad16(base + s * Ns)] = v[dr16(s)];
+}
+
+// The full M-point FFT of the values in `buf` (natural order, padded), or, for
+// the forward transform, of v[] already loaded for pass 1 (LOADED).  Result in
+// `buf`, natural order.  Every thread of the block calls it.
+template <bool INV, int M, bool LOADED>
+__device__ __forceinline__ void reg_fft(float2 (&v)[16], float2 *buf, const float2 *__restrict__ W) {
+    constexpr int T = M / 16;
+    const int j = threadIdx.x;
+    int Ns = 1;
+    if (!LOADED) {
+#pragma unroll
+        for (int r = 0; r < 16; r++) v[r] = buf[pad16(j + r * T)];
+        __syncthreads();
+    }
+    pass16_compute_write<INV, M>(v, buf, j, 1, W);
+    __syncthreads();
+    Ns = 16;
+#pragma unroll 1
+    for (; Ns * 16 <= M; Ns *= 16) {
+#pragma unroll
+        for (int r = 0; r < 16; r++) v[r] = buf[pad16(j + r * T)];
+        __syncthreads();
+        pass16_compute_write<INV, M>(v, buf, j, Ns, W);
+        __syncthreads();
+    }
+    if (Ns < M) {
+        // last pass, radix R = M / Ns in {2, 4, 8}: 16 / R groups per thread, j' = j + T g;
+        // each group reads and writes only its own R elements (j' + r M/R = j' + r Ns)
+        constexpr int dummy = 0;
+        (void)dummy;
+        const int R = M / Ns;
+        const int step = (2 * M) / M;   // W_M^1 = W_N^2
+        for (int g = 0; g < 16 / R; g++) {
+            const int jj = j + T * g;   // jj < M / R = Ns, so k = jj
+            float2 a[8];
+            for (int r = 0; r < R; r++) a[r] = buf[pad16(jj + r * Ns)];
+            for (int r = 1; r < R; r++) {
+                float2 w = __ldg(&W[r * jj * step]);
+                if (INV) w = cconj(w);
+                a[r] = cmul(a[r], w);
+            }
+            if (R == 2) {
+                dft2<INV>(a[0], a[1]);
+            } else if (R == 4) {
+                dft4<INV>(a[0], a[1], a[2], a[3]);
+            } else {   // R == 8: two radix-4 over even/odd, then combine
+                dft4<INV>(a[0], a[2], a[4], a[6]);
+                dft4<INV>(a[1], a[3], a[5], a[7]);
+                const float2 w1 = make_float2(kR2, INV ? kR2 : -kR2);
+                const float2 w3 = make_float2(-kR2, INV ? kR2 : -kR2);
+                const float2 o1 = cmul(a[3], w1), o2 = rot_q<INV>(a[5]), o3 = cmul(a[7], w3);
+                const float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6], o0 = a[1];
+                a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
+                a[1] = cadd(e1, o1); a[5] = csub(e1, o1);
+                a[2] = cadd(e2, o2); a[6] = csub(e2, o2);
+                a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
+            }
+            for (int s = 0; s < R; s++) buf[pad16(jj + s * Ns)] = a[s];
+        }
+    }
+    __syncthreads();
+}
+
+template <int M>
+__global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
+        const float *__restrict__ rir, int P, int R, int L, int S, const float2 *__restrict__ W,
+        const float2 *__restrict__ Sg, float *__restrict__ out, long out_ld) {
+    constexpr int T = M / 16;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *buf = sm;   // pad16(M) elements
+    const int j = threadIdx.x;
+    const int n_out = S + L - 1;
+    float2 v[16];
+    for (int pr = blockIdx.x; pr < P * R; pr += gridDim.x) {
+        const int p = pr / R;
+        const float *x = rir + (size_t)pr * L;
+        // pass-1 inputs straight from global memory: z[n] = x[2n] + i x[2n+1], n = j + r T
+        if ((reinterpret_cast<uintptr_t>(x) & 7) == 0) {
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const int n = j + r * T;
+                if (2 * n + 1 < L) v[r] = __ldg(reinterpret_cast<const float2 *>(x) + n);
+                else v[r] = make_float2(2 * n < L ? __ldg(&x[2 * n]) : 0.0f, 0.0f);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                const int n = j + r * T;
+                v[r] = make_float2(2 * n < L ? __ldg(&x[2 * n]) : 0.0f, 2 * n + 1 < L ? __ldg(&x[2 * n + 1]) : 0.0f);
+            }
+        }
+        reg_fft<false, M, true>(v, buf, W);
+        // spectrum of the RIR at k and M - k, times the segment's spectrum, repacked
+        // for the inverse real FFT (same algebra as rir_conv_kernel)
+        const float2 *sp = Sg + (size_t)p * (M + 1);
+        for (int k = j; k <= M / 2; k += T) {
+            const int km = (M - k) & (M - 1);
+            const float2 zk = buf[pad16(k)], zm = buf[pad16(km)];
+            const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+            const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+            const float2 wk = __ldg(&W[k]);
+            const float2 wm = make_float2(-wk.x, wk.y);
+            const float2 yk = cmul(cadd(ze, cmul(wk, zo)), __ldg(&sp[k]));
+            const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), __ldg(&sp[M - k]));
+            const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
+            const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
+            buf[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
+            if (k != 0 && km != k) {
+                const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
+                const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
+                buf[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+            }
+        }
+        __syncthreads();
+        reg_fft<true, M, false>(v, buf, W);
+        float *o = out + (size_t)pr * out_ld;
+        for (int i = j; i < n_out; i += T) {
+            const float2 z = buf[pad16(i >> 1)];
+            o[i] = (i & 1) ? z.y : z.x;
+        }
+        __syncthreads();
+    }
+}
+
+template <int M>
+static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S, const float2 *W,
+                                   const float2 *Sg, float *out, long out_ld, cudaStream_t st) {
+    const size_t smem = (size_t)(M + M / 16) * sizeof(float2);
+    static int blocks = -1;
+    if (blocks < 0) {
+        cudaError_t e = cudaFuncSetAttribute(rir_conv_reg_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rir_conv_reg_kernel<M>, M / 16, smem);
+        if (e != cudaSuccess) return e;
+        blocks = std::max(1, per_sm) * std::max(1, sms);
+    }
+    const int grid = std::min(P * R, blocks);
+    rir_conv_reg_kernel<M><<<grid, M / 16, smem, st>>>(rir, P, R, L, S, W, Sg, out, out_ld);
+    return cudaGetLastError();
+}
+
 // Overlap-add (gpuRIR/__init__.py:216-219): out[t][r] = sum over points p, in
 // increasing p, of conv[p][r][t - w_ini[p]] for 0 <= t - w_ini[p] < w_len[p] + L - 1.
 // Compensated FP32 sum (two-sum), written as float64.
@@ -272,6 +515,13 @@ cudaError_t segment_spectra_launch(const float *seg, int P, int S, int M, const 
 cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M, const float2 *W,
                             const float2 *Sg, float *out, long out_ld, float2 *scratch, int grid,
                             cudaStream_t st) {
+    switch (M) {   // register-resident kernel for the common sizes
+    case 1024: return launch_reg_conv<1024>(rir, P, R, L, S, W, Sg, out, out_ld, st);
+    case 2048: return launch_reg_conv<2048>(rir, P, R, L, S, W, Sg, out, out_ld, st);
+    case 4096: return launch_reg_conv<4096>(rir, P, R, L, S, W, Sg, out, out_ld, st);
+    case 8192: return launch_reg_conv<8192>(rir, P, R, L, S, W, Sg, out, out_ld, st);
+    default: break;
+    }
     cudaError_t e = set_fft_smem();
     if (e != cudaSuccess) return e;
     rir_conv_kernel<<<grid, kFftThreads, fft_smem_bytes(M), st>>>(rir, P, R, L, S, M, W, Sg, out, out_ld,
