@@ -977,6 +977,10 @@ static int ensure_conv(gpurir_sim *s, size_t bytes) {
     return GPURIR_OK;
 }
 
+// Row pitch of the intermediate convolution rows: whole float4s, so that the
+// convolution kernel stores them 16 bytes at a time.
+static long conv_ld(long n) { return (n + 3) & ~3L; }
+
 struct ConvPlan {
     int N, M, grid_seg, grid_conv;
     size_t o_sg, o_scr, o_conv, o_win, o_in_seg, o_in_rir, bytes;
@@ -998,7 +1002,7 @@ static int plan_conv(gpurir_sim *s, int P, int S, int R, int L, bool need_conv, 
     C.o_sg = 0;
     C.o_scr = align_up(C.o_sg + (size_t)P * (C.M + 1) * sizeof(float2), 256);
     C.o_conv = align_up(C.o_scr + fft_scratch_floats2(C.M, grid_scr) * sizeof(float2), 256);
-    C.o_win = align_up(C.o_conv + (need_conv ? (size_t)P * R * n * sizeof(float) : 0), 256);
+    C.o_win = align_up(C.o_conv + (need_conv ? (size_t)P * R * conv_ld(n) * sizeof(float) : 0), 256);
     C.o_in_seg = align_up(C.o_win + (need_win ? (size_t)2 * (P + 1) * sizeof(int) : 0), 256);
     C.o_in_rir = align_up(C.o_in_seg + (stage_inputs ? (size_t)P * S * sizeof(float) : 0), 256);
     C.bytes = align_up(C.o_in_rir + (stage_inputs ? (size_t)P * R * L * sizeof(float) : 0), 256);
@@ -1100,8 +1104,8 @@ static int trajectory_core(gpurir_sim *s, const float *d_seg, int n_pts, int seg
     s->stage_pending = true;
     const long n = (long)seg_len + rir_len - 1;
     float *conv = reinterpret_cast<float *>(s->d_conv + C.o_conv);
-    if ((rc = run_conv(s, C, d_seg, n_pts, seg_len, d_rir, n_rcv, rir_len, conv, n, st))) return rc;
-    CK(ola_launch(conv, n, dwin, dwin + n_pts + 1, n_pts, n_rcv, rir_len,
+    if ((rc = run_conv(s, C, d_seg, n_pts, seg_len, d_rir, n_rcv, rir_len, conv, conv_ld(n), st))) return rc;
+    CK(ola_launch(conv, conv_ld(n), dwin, dwin + n_pts + 1, n_pts, n_rcv, rir_len,
                   (long)w_ini[n_pts] + rir_len - 1, d_out, st));
     CK(cudaEventRecord(s->conv_busy, st));
     s->conv_recorded = true;

@@ -380,9 +380,19 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
     const int j = threadIdx.x;
     const int n_out = S + L - 1;
     float2 v[16];
+    const bool vec_out = (out_ld & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
     for (int pr = blockIdx.x; pr < P * R; pr += gridDim.x) {
         const int p = pr / R;
         const float *x = rir + (size_t)pr * L;
+        if (j == 0 && pr + (int)gridDim.x < P * R) {
+            // the block's next RIR row into L2 while this row is transformed (whole
+            // 16-byte units inside the row only)
+            const uintptr_t a = reinterpret_cast<uintptr_t>(rir + (size_t)(pr + gridDim.x) * L);
+            const uintptr_t lo = (a + 15) & ~(uintptr_t)15, hi = (a + (size_t)L * sizeof(float)) & ~(uintptr_t)15;
+            if (hi > lo)
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo))
+                             : "memory");
+        }
         // pass-1 inputs straight from global memory: z[n] = x[2n] + i x[2n+1], n = j + r T
         if ((reinterpret_cast<uintptr_t>(x) & 7) == 0) {
 #pragma unroll
@@ -424,9 +434,16 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
         __syncthreads();
         reg_fft<true, M, false>(v, buf, W);
         float *o = out + (size_t)pr * out_ld;
-        for (int i = j; i < n_out; i += T) {
-            const float2 z = buf[pad16(i >> 1)];
-            o[i] = (i & 1) ? z.y : z.x;
+        if (vec_out) {   // rows padded to whole float4: the 0..3 floats past n_out land in the padding
+            for (int q = j; 4 * q < n_out; q += T) {
+                const float2 z0 = buf[pad16(2 * q)], z1 = buf[pad16(2 * q + 1)];
+                reinterpret_cast<float4 *>(o)[q] = make_float4(z0.x, z0.y, z1.x, z1.y);
+            }
+        } else {
+            for (int i = j; i < n_out; i += T) {
+                const float2 z = buf[pad16(i >> 1)];
+                o[i] = (i & 1) ? z.y : z.x;
+            }
         }
         __syncthreads();
     }

@@ -22,10 +22,15 @@ def segment_signal(source_signal, n_pts, timestamps=None, fs=None):
         timestamps = np.arange(n_pts)
     w_ini = np.append((np.asarray(timestamps) * fs).astype(int), n)
     w_len = np.diff(w_ini)
-    segments = np.zeros((n_pts, w_len.max()))
-    for p in range(n_pts):
-        segments[p, 0:w_len[p]] = source_signal[w_ini[p]:w_ini[p + 1]]
-    return segments.astype('float32', order='C', copy=False), w_ini, w_len
+    width = int(w_len.max())
+    sig = np.asarray(source_signal)
+    if np.all(w_len == width) and np.array_equal(w_ini[:-1], width * np.arange(n_pts)):
+        segments = sig[:n_pts * width].reshape(n_pts, width).astype(np.float32)   # back to back
+    else:
+        segments = np.zeros((n_pts, width), dtype=np.float32)
+        for p in range(n_pts):
+            segments[p, 0:w_len[p]] = sig[w_ini[p]:w_ini[p + 1]]
+    return np.ascontiguousarray(segments), w_ini, w_len
 
 
 def gpu_conv(source_segments, RIRs, sim=None):
