@@ -242,7 +242,8 @@ static int build_room(RoomDesc &R, const float room[3], const float beta[6], con
         R.nb[d] = nb[d];
     }
     long long nimg = (long long)nb[0] * nb[1] * nb[2];
-    if (nimg > (1LL << 30)) return fail(GPURIR_ERR_INVALID, "too many images (nb_img product > 2^30)");
+    // the kernels split image indices with float arithmetic: exact below 2^24
+    if (nimg > (1LL << 24)) return fail(GPURIR_ERR_UNSUPPORTED, "too many images (nb_img product > 2^24)");
     for (int w = 0; w < 6; w++) {
         if (!std::isfinite(beta[w])) return fail(GPURIR_ERR_INVALID, "beta must be finite");
         R.beta[w] = beta[w];

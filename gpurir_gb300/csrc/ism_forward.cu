@@ -78,6 +78,48 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
+// sin(pi f) for 0 <= f <= 1: reflected to g = min(f, 1 - f) <= 1/2 (1 - f is exact
+// there), then the Taylor series of sin(pi g) = g * sum_k (-1)^k pi^(2k+1) g^(2k) / (2k+1)!
+// through k = 7 (remainder < 1e-9 relative), Horner in g^2.
+__device__ __forceinline__ float sinpi_unit(float f) {
+    const float g = fminf(f, 1.0f - f);
+    const float y = g * g;
+    float p = -2.1915353447830215827e-05f;
+    p = fmaf(p, y, 4.6630280576761256442e-04f);
+    p = fmaf(p, y, -7.3704309457143507773e-03f);
+    p = fmaf(p, y, 8.2145886611128228799e-02f);
+    p = fmaf(p, y, -5.9926452932079207689e-01f);
+    p = fmaf(p, y, 2.5501640398773454439f);
+    p = fmaf(p, y, -5.1677127800499700292f);
+    p = fmaf(p, y, 3.1415926535897932385f);
+    return g * p;
+}
+
+// sin(pi u), cos(pi u) for 0 <= u <= 1/16 by their Taylor series (remainders below
+// 1e-12 absolute): the per-image window angle, u = f / H.
+__device__ __forceinline__ void sincospi_small(float u, float &sn, float &cs) {
+    const float y = u * u;
+    float ps = -5.9926452932079207689e-01f;
+    ps = fmaf(ps, y, 2.5501640398773454439f);
+    ps = fmaf(ps, y, -5.1677127800499700292f);
+    ps = fmaf(ps, y, 3.1415926535897932385f);
+    sn = u * ps;
+    float pc = 2.3533063035889320454e-01f;
+    pc = fmaf(pc, y, -1.3352627688545894959f);
+    pc = fmaf(pc, y, 4.0587121264167682182f);
+    pc = fmaf(pc, y, -4.9348022005446793094f);
+    cs = fmaf(pc, y, 1.0f);
+}
+
+// q = n / d, r = n - q d for 0 <= n < 2^24, 1 <= d: float reciprocal, then an exact
+// fix-up of the (at most a few units) rounding error.
+__device__ __forceinline__ void divmod_small(int n, int d, float rd, int &q, int &r) {
+    q = (int)((float)n * rd);
+    r = n - q * d;
+    while (r < 0) { q -= 1; r += d; }
+    while (r >= d) { q += 1; r -= d; }
+}
+
 // Taps of one image into its sub-range buffer: lane l owns taps
 // k = k_lo + l + 32 i, i < TPL, at p[32 i].  With x = k - f the Hann window is
 //   0.5 (1 + cos(2 pi x / Tw)) = 0.5 + [0.5 cos(2 pi k/Tw)] cos(phi) + [0.5 sin(2 pi k/Tw)] sin(phi),
@@ -234,6 +276,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const int n_img = R.n_img;
         const float H = R.H;
         const float inv_h = 1.0f / H;
+        const float rN1 = 1.0f / (float)N1, rN2 = 1.0f / (float)N2;
+        const bool small_phi = inv_h <= 0.0625f;   // window angle f / H <= 1/16: polynomials
         const int k_lo = (int)floorf(-H) + 1;
         const int spkr = R.spkr, mic = R.mic;
         const ff kfs = {R.kh, R.kl};
@@ -279,55 +323,66 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 float a = 0.f, f = 0.f, sphi = 0.f, cphi = 1.f;
                 int n0 = 0;
                 if (i < n_img) {
-                    const int q = i / N2;
-                    const int m2 = i - q * N2;
-                    const int m0 = q / N1;
-                    const int m1 = q - m0 * N1;
+                    int q, m2, m0, m1;
+                    divmod_small(i, N2, rN2, q, m2);
+                    divmod_small(q, N1, rN1, m0, m1);
                     int c0, r0, c1, r1, c2, r2;
                     image_axis(m0, N0, c0, r0);
                     image_axis(m1, N1, c1, r1);
                     image_axis(m2, N2, c2, r2);
-                    const float att = __ldg(&R.pw[0][abs(c0 - r0)]) * __ldg(&R.pw[1][abs(c0)]) *
-                                      __ldg(&R.pw[2][abs(c1 - r1)]) * __ldg(&R.pw[3][abs(c1)]) *
-                                      __ldg(&R.pw[4][abs(c2 - r2)]) * __ldg(&R.pw[5][abs(c2)]);
                     // vector receiver -> image, float-float (src/gpuRIR_cuda.cu:353)
                     const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
                     const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
                     const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
                     const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
-                    const ff dist = ff_sqrt(d2);
-                    const ff tau = ff_mul(dist, kfs);
-                    const float inv_d = 1.0f / dist.hi;
-                    float amp = att * (0.0795774715459476679f * inv_d);   // 1/(4 pi dist)
-                    if (spkr != P_OMNI) {
-                        // doa = image -> receiver = -vec; axis mirrored per reflection (:357-362)
-                        float ct = -((r0 ? -os0 : os0) * v0.hi + (r1 ? -os1 : os1) * v1.hi +
-                                     (r2 ? -os2 : os2) * v2.hi) * inv_d;
-                        amp *= pattern_gain(ct, spkr);
-                    }
-                    if (mic != P_OMNI) {
-                        float ct = (or0 * v0.hi + or1 * v1.hi + or2 * v2.hi) * inv_d;   // (:363)
-                        amp *= pattern_gain(ct, mic);
-                    }
-                    float fl = floorf(tau.hi);
-                    n0 = (int)fl;
-                    f = __fadd_rn(__fsub_rn(tau.hi, fl), tau.lo);
-                    if (f < 0.0f) { n0 -= 1; f += 1.0f; }
-                    if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
-                    f = fmaxf(f, 9.094947017729282e-13f);   // 2^-40: keeps x = k - f != 0
-                    if (MODE == kModeLUT) {
-                        // the reference stores tau as a float: split its nearest float
-                        fl = floorf(tau.hi);
+                    // approximate distance first: images whose delay is far outside this
+                    // segment (a third of them in a room's corner regions) stop here
+                    const float rs0 = rsqrtf(d2.hi);
+                    const float s0 = d2.hi * rs0;
+                    const float tau_est = s0 * kfs.hi;
+                    if (tau_est > keep_lo - 1.0f && tau_est < keep_hi + 1.0f) {
+                        const float att = __ldg(&R.pw[0][abs(c0 - r0)]) * __ldg(&R.pw[1][abs(c0)]) *
+                                          __ldg(&R.pw[2][abs(c1 - r1)]) * __ldg(&R.pw[3][abs(c1)]) *
+                                          __ldg(&R.pw[4][abs(c2 - r2)]) * __ldg(&R.pw[5][abs(c2)]);
+                        // distance = s0 + (d2 - s0^2) / (2 s0): one Newton step in float-float
+                        // (the residual by FMA is exact to ~1e-14 of d2)
+                        const float rs = rs0 * fmaf(-0.5f * d2.hi * rs0, rs0, 1.5f);   // 1/dist
+                        const float res = fmaf(-s0, s0, d2.hi) + d2.lo;
+                        const ff dist = ff_fast_two_sum(s0, 0.5f * res * rs);
+                        const ff tau = ff_mul(dist, kfs);
+                        const float inv_d = rs;
+                        float amp = att * (0.0795774715459476679f * inv_d);   // 1/(4 pi dist)
+                        if (spkr != P_OMNI) {
+                            // doa = image -> receiver = -vec; axis mirrored per reflection (:357-362)
+                            float ct = -((r0 ? -os0 : os0) * v0.hi + (r1 ? -os1 : os1) * v1.hi +
+                                         (r2 ? -os2 : os2) * v2.hi) * inv_d;
+                            amp *= pattern_gain(ct, spkr);
+                        }
+                        if (mic != P_OMNI) {
+                            float ct = (or0 * v0.hi + or1 * v1.hi + or2 * v2.hi) * inv_d;   // (:363)
+                            amp *= pattern_gain(ct, mic);
+                        }
+                        float fl = floorf(tau.hi);
                         n0 = (int)fl;
-                        f = tau.hi - fl;   // exact
-                        a = amp;
-                    } else {
-                        a = -amp * sinpif(f) * 0.318309886183790672f;
-                        sincospif(f * inv_h, &sphi, &cphi);   // phi = 2 pi f / Tw
-                    }
-                    if (amp != 0.0f && tau.hi > keep_lo && tau.hi < keep_hi) {
-                        int rel = n0 - t_lo;
-                        sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
+                        f = __fadd_rn(__fsub_rn(tau.hi, fl), tau.lo);
+                        if (f < 0.0f) { n0 -= 1; f += 1.0f; }
+                        if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
+                        f = fmaxf(f, 9.094947017729282e-13f);   // 2^-40: keeps x = k - f != 0
+                        if (MODE == kModeLUT) {
+                            // the reference stores tau as a float: split its nearest float
+                            fl = floorf(tau.hi);
+                            n0 = (int)fl;
+                            f = tau.hi - fl;   // exact
+                            a = amp;
+                        } else {
+                            a = -amp * sinpi_unit(f) * 0.318309886183790672f;
+                            if (small_phi) sincospi_small(f * inv_h, sphi, cphi);   // phi = 2 pi f / Tw
+                            else sincospif(f * inv_h, &sphi, &cphi);
+                        }
+                        if (amp != 0.0f && tau.hi > keep_lo && tau.hi < keep_hi) {
+                            int rel = n0 - t_lo;
+                            sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
+                        }
                     }
                 }
                 rec[local] = make_float4(a, f, cphi, sphi);
