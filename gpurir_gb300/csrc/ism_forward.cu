@@ -401,12 +401,16 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 for (int h = 0; h < 2; h++) {
                     const int s = lane + 32 * h;
                     int run = 0;
-                    if (s < nsub)
+                    if (s < nsub) {
+                        int c[kWarps];   // independent loads, then the running sum in registers
+#pragma unroll
+                        for (int w = 0; w < kWarps; w++) c[w] = hist[w * kMaxSub + s];
+#pragma unroll
                         for (int w = 0; w < kWarps; w++) {
-                            const int c = hist[w * kMaxSub + s];
                             hist[w * kMaxSub + s] = run;
-                            run += c;
+                            run += c[w];
                         }
+                    }
                     cnt2[h] = run;
                 }
                 int x0 = cnt2[0], x1 = cnt2[1];
@@ -441,20 +445,20 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 const int n_extra = etot0 + __shfl_sync(0xffffffffu, e1, 31);
                 const int fpre[2] = {f0 - full2[0], ftot0 + f1 - full2[1]};
                 const int epre[2] = {e0 - ext2[0], etot0 + e1 - ext2[1]};
-                // remainder slices ranked by (size desc, s asc)
-                int rk[2] = {0, 0};
-                for (int t = 0; t < 64; t++) {
-                    const int rt = __shfl_sync(0xffffffffu, t < 32 ? rem2[0] : rem2[1], t & 31);
-                    if (t < nsub && rt > 0) {
-                        rk[0] += (rt > rem2[0]) || (rt == rem2[0] && t < lane);
-                        rk[1] += (rt > rem2[1]) || (rt == rem2[1] && t < lane + 32);
-                    }
-                }
-                int n_rem = 0;
-                for (int t = 0; t < 64; t++) {
-                    const int rt = __shfl_sync(0xffffffffu, t < 32 ? rem2[0] : rem2[1], t & 31);
-                    n_rem += (t < nsub && rt > 0);
-                }
+                // remainder slices: those of at least half a slice first, then the smaller
+                // ones, each class in s order (ballot ranks: no serial loop)
+                const int half = (cap + 1) / 2;
+                const bool v0 = lane < nsub, v1 = lane + 32 < nsub;
+                const unsigned a0 = __ballot_sync(0xffffffffu, v0 && rem2[0] >= half);
+                const unsigned a1 = __ballot_sync(0xffffffffu, v1 && rem2[1] >= half);
+                const unsigned b0 = __ballot_sync(0xffffffffu, v0 && rem2[0] > 0 && rem2[0] < half);
+                const unsigned b1 = __ballot_sync(0xffffffffu, v1 && rem2[1] > 0 && rem2[1] < half);
+                const int n_a = __popc(a0) + __popc(a1);
+                const int n_rem = n_a + __popc(b0) + __popc(b1);
+                int rk[2];
+                rk[0] = rem2[0] >= half ? __popc(a0 & lt_mask) : n_a + __popc(b0 & lt_mask);
+                rk[1] = rem2[1] >= half ? __popc(a0) + __popc(a1 & lt_mask)
+                                        : n_a + __popc(b0) + __popc(b1 & lt_mask);
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int s = lane + 32 * h;
