@@ -37,6 +37,8 @@ constexpr int kRounds = kPerWarp / 32;              // 32-image rounds per warp 
 constexpr int kMaxSub = 64;                         // sub-ranges per item
 constexpr int kPool = kWarps;                       // extra slices of heavy sub-ranges per chunk
 constexpr int kMaxItems = 128;                      // >= kMaxSub + kPool queue entries
+constexpr short kNoImage = -32768;                  // record of an image outside the segment
+static_assert(kPerWarp <= 256, "ranks within a warp's bucket are stored in 8 bits");
 static_assert(kThreads == kPowerThreads, "the fused tail sums the window power in the tail kernel's order");
 
 struct IsmLaunch {
@@ -213,8 +215,9 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     float4 *rec = reinterpret_cast<float4 *>(smem_raw);            // [kChunk] a, f, cos phi, sin phi
     short *rec_n0 = reinterpret_cast<short *>(rec + kChunk);        // [kChunk] floor(tau) - t_lo
     unsigned short *perm = reinterpret_cast<unsigned short *>(rec_n0 + kChunk);  // [kChunk]
-    signed char *rec_sub = reinterpret_cast<signed char *>(perm + kChunk);       // [kChunk]
-    int *hist = reinterpret_cast<int *>(rec_sub + kChunk);          // [kWarps][kMaxSub]
+    // [kChunk] rank of the image among its warp's images of the same sub-range (< kPerWarp)
+    unsigned char *rec_rank = reinterpret_cast<unsigned char *>(perm + kChunk);
+    int *hist = reinterpret_cast<int *>(rec_rank + kChunk);         // [kWarps][kMaxSub]
     int *sub_start = hist + kWarps * kMaxSub;
     int *sub_cnt = sub_start + kMaxSub;
     int *pool_base = sub_cnt + kMaxSub;                                        // first pool slot of s
@@ -386,10 +389,13 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     }
                 }
                 rec[local] = make_float4(a, f, cphi, sphi);
-                rec_n0[local] = (short)(sub >= 0 ? n0 - t_lo : 0);   // |.| < 2^15: host caps segments
-                rec_sub[local] = (signed char)sub;
+                // n0 - t_lo (|.| < 2^15: host caps segments), kNoImage for images outside
+                rec_n0[local] = (short)(sub >= 0 ? n0 - t_lo : kNoImage);
                 const unsigned peers = __match_any_sync(0xffffffffu, sub);
+                const int rank = sub >= 0 ? my_hist[sub] + __popc(peers & lt_mask) : 0;
+                __syncwarp();
                 if (sub >= 0 && (peers & lt_mask) == 0) my_hist[sub] += __popc(peers);
+                rec_rank[local] = (unsigned char)rank;
                 __syncwarp();
             }
             __syncthreads();
@@ -484,12 +490,11 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 #pragma unroll 1
             for (int r = 0; r < kRounds; r++) {
                 const int local = warp * kPerWarp + r * 32 + lane;
-                const int sub = rec_sub[local];
-                const unsigned peers = __match_any_sync(0xffffffffu, sub);
-                if (sub >= 0) perm[my_hist[sub] + __popc(peers & lt_mask)] = (unsigned short)local;
-                __syncwarp();
-                if (sub >= 0 && (peers & lt_mask) == 0) my_hist[sub] += __popc(peers);
-                __syncwarp();
+                const int rel = rec_n0[local];
+                if (rel != kNoImage) {   // the sub-range as pass 1 derived it from rel
+                    const int sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
+                    perm[my_hist[sub] + rec_rank[local]] = (unsigned short)local;
+                }
             }
             __syncthreads();
             // ---- pass 3: warps pull slices, scatter taps into private buffers
