@@ -126,22 +126,24 @@ __device__ __forceinline__ void divmod_small(int n, int d, float rd, int &q, int
 // k = k_lo + l + 32 i, i < TPL, at p[32 i].  With x = k - f the Hann window is
 //   0.5 (1 + cos(2 pi x / Tw)) = 0.5 + [0.5 cos(2 pi k/Tw)] cos(phi) + [0.5 sin(2 pi k/Tw)] sin(phi),
 // phi = 2 pi f / Tw: the bracketed factors are per-lane constants (ck, sk) and
-// (cos phi, sin phi) comes with the image, so a tap costs one FADD, two FFMA,
-// one MUFU.RCP, one FMUL and the shared-memory accumulate.
+// (cos phi, sin phi) comes with the image.  In FP32 mode the image's amplitude is
+// folded in as well: the record holds (a, f, a cos phi, a sin phi), ck and sk carry
+// the lane's sign (-1)^k, and al = 0.5 a (-1)^k, so a tap is
+//   acc += (al + ck (a cos phi) + sk (a sin phi)) / x:
+// one FADD, two FFMA, one MUFU.RCP, one FFMA and the shared-memory read and write.
 template <int TPL, bool CLAMP, int MODE>
 __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], const float (&ck)[TPL],
                                              const float (&sk)[TPL], float al, float4 r, float H,
                                              const float2 *lut, int lut_cols) {
     const float f = r.y;
     if (MODE == kModeF32) {
-        const float cphi = r.z, sphi = r.w;
+        const float ac = r.z, as = r.w;   // a cos phi, a sin phi
 #pragma unroll
         for (int i = 0; i < TPL; i++) {
             const float x = kf[i] - f;
-            const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
-            float v = w * rcp_approx(x);
-            if (CLAMP) v = fabsf(x) < H ? v : 0.0f;
-            p[32 * i] = fmaf(al, v, p[32 * i]);
+            float u = fmaf(ck[i], ac, fmaf(sk[i], as, al));
+            if (CLAMP) u = fabsf(x) < H ? u : 0.0f;
+            p[32 * i] = fmaf(u, rcp_approx(x), p[32 * i]);
         }
     } else if (MODE == kModeMP) {
         const __half2 cphi = __float2half2_rn(r.z), sphi = __float2half2_rn(r.w);
@@ -310,8 +312,10 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             sincospif(kf[i] * inv_h, &sn, &cs);   // 2 pi k / Tw = pi k / H
             ck[i] = 0.5f * cs;
             sk[i] = 0.5f * sn;
+            if (MODE == kModeF32 && ((k_lo + lane) & 1)) { ck[i] = -ck[i]; sk[i] = -sk[i]; }
         }
-        const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
+        // (-1)^k of the lane's taps, times 1/2 in FP32 mode (the window's constant term)
+        const float lane_sign = (((k_lo + lane) & 1) ? -1.0f : 1.0f) * (MODE == kModeF32 ? 0.5f : 1.0f);
         int *my_hist = hist + warp * kMaxSub;
 
         for (int cbase = 0; cbase < n_img; cbase += kChunk) {
@@ -381,6 +385,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                             a = -amp * sinpi_unit(f) * 0.318309886183790672f;
                             if (small_phi) sincospi_small(f * inv_h, sphi, cphi);   // phi = 2 pi f / Tw
                             else sincospif(f * inv_h, &sphi, &cphi);
+                            if (MODE == kModeF32) { cphi *= a; sphi *= a; }   // record a cos phi, a sin phi
                         }
                         if (amp != 0.0f && tau.hi > keep_lo && tau.hi < keep_hi) {
                             int rel = n0 - t_lo;
