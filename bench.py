@@ -365,13 +365,14 @@ def run_gpu(a):
 
     for _ in range(max(2, a.warmup // 2)):
         host_step()
-    e2e_s = 0.0
+    e2e_s, e2e_kernel_ms = 0.0, 0.0
     for _ in range(a.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         host_step()
         e2e_s += time.perf_counter() - t0
+        e2e_kernel_ms += sim.last_timing()[0]
     h2d, d2h = sim.last_transfer_bytes()
     direct = sim.last_output_direct()
     if world > 1:
@@ -416,6 +417,7 @@ def run_gpu(a):
             "kernel_ms": {"ism_forward": ism_avg, "tail": sum(tail_ms) / len(tail_ms)},
             "e2e": {"value": e2e_value, "unit": "RIRs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3,
+                    "kernel_ms": e2e_kernel_ms / a.steps,
                     "d2h": "kernel stores into the pinned host buffer over NVLink-C2C" if direct
                            else "cudaMemcpyAsync after the kernels"},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches}

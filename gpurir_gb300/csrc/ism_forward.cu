@@ -552,17 +552,33 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
             w_start = envelope_start(R, tau_dp);
         }
+        // four consecutive samples per thread (t_lo is a multiple of 4): 16-byte stores
+        // where the row allows, which also suits stores into host memory
         float pw = 0.0f;
-        for (int t = t_lo + tid; t < t_hi; t += kThreads) {
-            const int rel = t - t_lo;
-            int s_max = (rel - k_lo) / SUB;
-            if (s_max > nsub - 1) s_max = nsub - 1;
-            int num = rel - k_lo - BUF + 1;   // buffer s covers rel in [s*SUB + k_lo, s*SUB + k_lo + BUF)
-            int s_min = num <= 0 ? 0 : (num + SUB - 1) / SUB;
-            float acc = 0.0f;
-            for (int s = s_min; s <= s_max; s++) acc += buf[P.em + s * BUF + rel - s * SUB - k_lo];
-            orow[t] = acc;
-            if (t >= w_start) pw = fmaf(acc, acc, pw);
+        const bool vec_out = (reinterpret_cast<uintptr_t>(orow + t_lo) & 15) == 0;
+        for (int t0 = t_lo + 4 * tid; t0 < t_hi; t0 += 4 * kThreads) {
+            float v[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int rel = t0 + e - t_lo;
+                int s_max = (rel - k_lo) / SUB;
+                if (s_max > nsub - 1) s_max = nsub - 1;
+                int num = rel - k_lo - BUF + 1;   // buffer s covers rel in [s*SUB + k_lo, s*SUB + k_lo + BUF)
+                int s_min = num <= 0 ? 0 : (num + SUB - 1) / SUB;
+                float acc = 0.0f;
+                for (int s = s_min; s <= s_max; s++) acc += buf[P.em + s * BUF + rel - s * SUB - k_lo];
+                v[e] = acc;
+            }
+            if (vec_out && t0 + 3 < t_hi) {
+                *reinterpret_cast<float4 *>(orow + t0) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (t0 + e < t_hi) orow[t0 + e] = v[e];
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                if (t0 + e >= w_start && t0 + e < t_hi) pw = fmaf(v[e], v[e], pw);
         }
         if (fuse) {
             float *red = reinterpret_cast<float *>(hist);   // free until the next item

@@ -42,10 +42,16 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
     const float tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
     const int w_start = envelope_start(R, tau_dp);
     float p = 0.0f;
-    for (int t = (w_start / kTailThreads) * kTailThreads + threadIdx.x; t < n_ism; t += kTailThreads) {
-        if (t < w_start) continue;
-        float v = row[t];
-        p = fmaf(v, v, p);
+    for (int t0 = (w_start / (4 * kTailThreads)) * (4 * kTailThreads) + 4 * threadIdx.x; t0 < n_ism;
+         t0 += 4 * kTailThreads) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int t = t0 + e;
+            if (t >= w_start && t < n_ism) {
+                const float v = row[t];
+                p = fmaf(v, v, p);
+            }
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);

@@ -9,10 +9,10 @@
 namespace gpurir {
 
 // Threads that sum the envelope-window power.  Thread j adds the squares of the
-// samples t = j (mod kPowerThreads), t >= w_start, in increasing t; warps then
-// combine by an xor butterfly and thread 0 adds the warp sums in order.  The
-// tail kernel and the ISM epilogue both follow this order, so an RIR's tail is
-// the same bits whichever of them writes it.
+// samples t >= w_start of the groups of four t / 4 = j (mod kPowerThreads), in
+// increasing t; warps then combine by an xor butterfly and thread 0 adds the warp
+// sums in order.  The tail kernel and the ISM epilogue both follow this order, so
+// an RIR's tail is the same bits whichever of them writes it.
 constexpr int kPowerThreads = 512;
 
 // Direct-path delay in samples, the float-float arithmetic the ISM kernel
