@@ -368,7 +368,10 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     const long seg_max = std::min<long>((long)max_nsub * sub, 16384);   // int16 image offsets
     const long target = 4L * s->num_sms;
     const long want = (target + M_tot - 1) / std::max<long>(M_tot, 1);
-    std::vector<std::pair<double, IsmItem>> work;
+    std::vector<IsmItem> work;
+    std::vector<std::pair<double, int>> cost;   // (estimated cost, index into work)
+    work.reserve(M_tot);
+    cost.reserve(M_tot);
     P.nsub = 1;
     for (size_t ri = 0; ri < R.size(); ri++) {
         const RoomDesc &r = R[ri];
@@ -402,17 +405,20 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
                 // images in the segment's delay range (density grows with delay^2), plus
                 // the geometry pass over every image of the room
                 const double a = (double)w.t_lo / r.n_ism, b = (double)w.t_hi / r.n_ism;
-                const double cost = r.n_img * ((b * b * b - a * a * a) + 0.15);
-                work.push_back({cost, w});
+                cost.push_back({r.n_img * ((b * b * b - a * a * a) + 0.15), (int)work.size()});
+                work.push_back(w);
             }
         }
     }
-    std::stable_sort(work.begin(), work.end(),
-                     [](const std::pair<double, IsmItem> &x, const std::pair<double, IsmItem> &y) {
-                         return x.first > y.first;
-                     });
+    // largest first, ties in plan order; a single room cut into one segment per RIR
+    // (all costs equal) is already in that order
+    bool sorted = true;
+    for (size_t i = 1; i < cost.size() && sorted; i++) sorted = cost[i - 1].first >= cost[i].first;
+    if (!sorted)
+        std::stable_sort(cost.begin(), cost.end(), [](const std::pair<double, int> &x,
+                                                      const std::pair<double, int> &y) { return x.first > y.first; });
     P.items.reserve(work.size());
-    for (auto &w : work) P.items.push_back(w.second);
+    for (auto &c : cost) P.items.push_back(work[c.second]);
     P.grid = 0;
     if (P.items.empty()) return GPURIR_OK;
     size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub, P.mode, P.tw);
