@@ -370,6 +370,59 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[16], float2 *buf, const floa
     __syncthreads();
 }
 
+// Pass-1 inputs of thread j straight from global memory: z[n] = x[2n] + i x[2n+1],
+// n = j + r M/16, zero past `len` (8-byte loads when the row allows).
+template <int M>
+__device__ __forceinline__ void load_packed(const float *__restrict__ x, int len, float2 (&v)[16]) {
+    constexpr int T = M / 16;
+    const int j = threadIdx.x;
+    if ((reinterpret_cast<uintptr_t>(x) & 7) == 0) {
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+            const int n = j + r * T;
+            if (2 * n + 1 < len) v[r] = __ldg(reinterpret_cast<const float2 *>(x) + n);
+            else v[r] = make_float2(2 * n < len ? __ldg(&x[2 * n]) : 0.0f, 0.0f);
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+            const int n = j + r * T;
+            v[r] = make_float2(2 * n < len ? __ldg(&x[2 * n]) : 0.0f, 2 * n + 1 < len ? __ldg(&x[2 * n + 1]) : 0.0f);
+        }
+    }
+}
+
+// Segment spectra with the register FFT: Sg[p][0..M] = FFT_N(segment p) / M.
+template <int M>
+__global__ void __launch_bounds__(M / 16, 16384 / M) segment_spectra_reg_kernel(
+        const float *__restrict__ seg, int P, int S, const float2 *__restrict__ W, float2 *__restrict__ Sg) {
+    constexpr int T = M / 16;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *buf = sm;
+    const int j = threadIdx.x;
+    const float scale = 1.0f / (float)M;
+    float2 v[16];
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        load_packed<M>(seg + (size_t)p * S, S, v);
+        reg_fft<false, M, true>(v, buf, W);
+        float2 *X = Sg + (size_t)p * (M + 1);
+        for (int k = j; k <= M / 2; k += T) {
+            const int km = (M - k) & (M - 1);
+            const float2 zk = buf[pad16(k)], zm = buf[pad16(km)];
+            const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+            const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+            const float2 wk = __ldg(&W[k]);
+            const float2 wm = make_float2(-wk.x, wk.y);
+            const float2 xk = cadd(ze, cmul(wk, zo));
+            const float2 xm = cadd(ze2, cmul(wm, zo2));
+            X[k] = make_float2(xk.x * scale, xk.y * scale);
+            X[M - k] = make_float2(xm.x * scale, xm.y * scale);
+        }
+        __syncthreads();
+    }
+}
+
 template <int M>
 __global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
         const float *__restrict__ rir, int P, int R, int L, int S, const float2 *__restrict__ W,
@@ -393,21 +446,7 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
                 asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo))
                              : "memory");
         }
-        // pass-1 inputs straight from global memory: z[n] = x[2n] + i x[2n+1], n = j + r T
-        if ((reinterpret_cast<uintptr_t>(x) & 7) == 0) {
-#pragma unroll
-            for (int r = 0; r < 16; r++) {
-                const int n = j + r * T;
-                if (2 * n + 1 < L) v[r] = __ldg(reinterpret_cast<const float2 *>(x) + n);
-                else v[r] = make_float2(2 * n < L ? __ldg(&x[2 * n]) : 0.0f, 0.0f);
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < 16; r++) {
-                const int n = j + r * T;
-                v[r] = make_float2(2 * n < L ? __ldg(&x[2 * n]) : 0.0f, 2 * n + 1 < L ? __ldg(&x[2 * n + 1]) : 0.0f);
-            }
-        }
+        load_packed<M>(x, L, v);
         reg_fft<false, M, true>(v, buf, W);
         // spectrum of the RIR at k and M - k, times the segment's spectrum, repacked
         // for the inverse real FFT (same algebra as rir_conv_kernel)
@@ -478,22 +517,30 @@ __global__ void ola_kernel(const float *conv, long conv_ld, const int *w_ini, co
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;   // consecutive t: coalesced reads
     const int r = blockIdx.y;
     if (t >= n_out) return;
-    // first point whose window may reach t: w_ini[p] + w_len[p] + L - 1 > t; points are sorted by w_ini
-    int lo = 0, hi = P;   // smallest p with w_ini[p] + w_len[p] + L - 1 > t
+    // points whose filtered segment covers t: lo = first p with w_ini[p] + w_len[p] + L - 1 > t,
+    // hi = first p with w_ini[p] > t (w_ini increasing, w_ini[p] + w_len[p] = w_ini[p + 1])
+    int lo = 0, hi = P;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if ((long)w_ini[mid] + w_len[mid] + L - 1 > t) hi = mid; else lo = mid + 1;
     }
+    int e = lo, e_hi = P;
+    while (e < e_hi) {
+        const int mid = (e + e_hi) >> 1;
+        if ((long)w_ini[mid] > t) e_hi = mid; else e = mid + 1;
+    }
+    // every p in [lo, e) contributes conv[p][r][t - w_ini[p]]: independent loads, then the
+    // compensated sum in increasing p
     float s = 0.0f, comp = 0.0f;
-    for (int p = lo; p < P && w_ini[p] <= t; p++) {
-        const long k = t - w_ini[p];
-        if (k < (long)w_len[p] + L - 1) {
-            const float v = conv[((long)p * R + r) * conv_ld + k];
-            const float y = s + v;                       // two-sum
-            const float bb = y - s;
-            comp += (s - (y - bb)) + (v - bb);
-            s = y;
-        }
+    const float *col = conv + (long)r * conv_ld + t;
+    const long pstride = (long)R * conv_ld;
+#pragma unroll 4
+    for (int p = lo; p < e; p++) {
+        const float v = __ldg(col + p * pstride - w_ini[p]);
+        const float y = s + v;                       // two-sum
+        const float bb = y - s;
+        comp += (s - (y - bb)) + (v - bb);
+        s = y;
     }
     out[t * R + r] = (double)s + (double)comp;
 }
@@ -521,8 +568,35 @@ static cudaError_t set_fft_smem() {
     return e;
 }
 
+template <int M>
+static cudaError_t launch_reg_spectra(const float *seg, int P, int S, const float2 *W, float2 *Sg,
+                                     cudaStream_t st) {
+    const size_t smem = (size_t)(M + M / 16) * sizeof(float2);
+    static int blocks = -1;
+    if (blocks < 0) {
+        cudaError_t e = cudaFuncSetAttribute(segment_spectra_reg_kernel<M>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, segment_spectra_reg_kernel<M>, M / 16, smem);
+        if (e != cudaSuccess) return e;
+        blocks = std::max(1, per_sm) * std::max(1, sms);
+    }
+    segment_spectra_reg_kernel<M><<<std::min(P, blocks), M / 16, smem, st>>>(seg, P, S, W, Sg);
+    return cudaGetLastError();
+}
+
 cudaError_t segment_spectra_launch(const float *seg, int P, int S, int M, const float2 *W, float2 *Sg,
                                    float2 *scratch, int grid, cudaStream_t st) {
+    switch (M) {   // register-resident kernel for the common sizes
+    case 1024: return launch_reg_spectra<1024>(seg, P, S, W, Sg, st);
+    case 2048: return launch_reg_spectra<2048>(seg, P, S, W, Sg, st);
+    case 4096: return launch_reg_spectra<4096>(seg, P, S, W, Sg, st);
+    case 8192: return launch_reg_spectra<8192>(seg, P, S, W, Sg, st);
+    default: break;
+    }
     cudaError_t e = set_fft_smem();
     if (e != cudaSuccess) return e;
     segment_spectra_kernel<<<grid, kFftThreads, fft_smem_bytes(M), st>>>(seg, P, S, M, W, Sg, scratch);
