@@ -210,3 +210,44 @@ def test_invalid_arguments_raise(built):
         sim.simulate_rir([3, 3, 3], [0.5] * 6, ps, ps, None, None, 0, 2, [3, 3, 3], 0.1, 0.1, 16000.0)
     with pytest.raises(G.GpuRirError):
         sim.simulate_rir([3, 3, 3], [0.5] * 6, ps, ps, None, None, 0, 0, [3, 3, 3], 0.2, 0.1, 16000.0)
+
+
+@pytest.mark.parametrize("fs", [96000.0, 11025.0])
+def test_high_and_odd_sample_rates(built, fs):
+    """96 kHz: a 768-tap window (24 taps per lane, the large shared-memory layout);
+    11.025 kHz: an odd 88-tap window (half-integer half width, clamped taps)."""
+    rng = np.random.default_rng(11)
+    room = [3.5, 3.0, 2.6]
+    ps = _rand_inside(rng, 1, room, 0.4)
+    pr = _rand_inside(rng, 2, room, 0.4)
+    out, ref, p = _run(_sim(), room, [0.75] * 6, ps, pr, [5, 5, 5], 0.03, fs)
+    _check_ism(out, ref, p["n_ism"], "fs %g" % fs)
+
+
+def test_window_beyond_supported_rate_is_an_error(built):
+    """Above ~190 kHz the window exceeds 24 taps per lane: refused, not truncated."""
+    import gpurir_gb300 as G
+    ps = np.array([[1, 1, 1]], dtype=np.float32)
+    pr = np.array([[2, 2, 1]], dtype=np.float32)
+    with pytest.raises(G.GpuRirError):
+        _sim().simulate_rir([3, 3, 3], [0.5] * 6, ps, pr, None, None, 0, 0, [3, 3, 3], 0.01, 0.01, 192000.0)
+
+
+def test_zero_lengths(built):
+    """Tmax = 0: an empty time axis; Tdiff = 0: no early part, and an empty envelope
+    window gives a silent tail (gpuRIR divides by <= 0 there)."""
+    sim = _sim()
+    ps = np.array([[1, 1, 1]], dtype=np.float32)
+    pr = np.array([[2, 2, 1.5], [2.5, 1.0, 1.0]], dtype=np.float32)
+    a = sim.simulate_rir([3, 3, 3], [0.8] * 6, ps, pr, None, None, 0, 0, [3, 3, 3], 0.0, 0.0, 16000.0)
+    assert a.shape == (1, 2, 0)
+    b = sim.simulate_rir([3, 3, 3], [0.8] * 6, ps, pr, None, None, 0, 0, [3, 3, 3], 0.0, 0.05, 16000.0)
+    assert b.shape == (1, 2, 800) and np.all(b == 0.0)
+
+
+def test_too_many_images_is_an_error(built):
+    import gpurir_gb300 as G
+    ps = np.array([[1, 1, 1]], dtype=np.float32)
+    with pytest.raises(G.GpuRirError):
+        _sim().simulate_rir([3, 3, 3], [0.5] * 6, ps, ps + 0.5, None, None, 0, 0, [300, 300, 300],
+                            0.01, 0.01, 16000.0)
