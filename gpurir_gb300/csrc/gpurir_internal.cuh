@@ -96,6 +96,88 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
 }
 
 // ---------------------------------------------------------------------------
+// Series evaluations and integer splits shared by the ISM kernels.
+// ---------------------------------------------------------------------------
+// sin(pi f) for 0 <= f <= 1: reflected to g = min(f, 1 - f) <= 1/2 (1 - f is exact
+// there), then the Taylor series of sin(pi g) = g * sum_k (-1)^k pi^(2k+1) g^(2k) / (2k+1)!
+// through k = 7 (remainder < 1e-9 relative), Horner in g^2.
+__device__ __forceinline__ float sinpi_unit(float f) {
+    const float g = fminf(f, 1.0f - f);
+    const float y = g * g;
+    float p = -2.1915353447830215827e-05f;
+    p = fmaf(p, y, 4.6630280576761256442e-04f);
+    p = fmaf(p, y, -7.3704309457143507773e-03f);
+    p = fmaf(p, y, 8.2145886611128228799e-02f);
+    p = fmaf(p, y, -5.9926452932079207689e-01f);
+    p = fmaf(p, y, 2.5501640398773454439f);
+    p = fmaf(p, y, -5.1677127800499700292f);
+    p = fmaf(p, y, 3.1415926535897932385f);
+    return g * p;
+}
+
+// sin(pi u), cos(pi u) for 0 <= u <= 1/16 by their Taylor series (remainders below
+// 1e-12 absolute): the per-image window angle, u = f / H.
+__device__ __forceinline__ void sincospi_small(float u, float &sn, float &cs) {
+    const float y = u * u;
+    float ps = -5.9926452932079207689e-01f;
+    ps = fmaf(ps, y, 2.5501640398773454439f);
+    ps = fmaf(ps, y, -5.1677127800499700292f);
+    ps = fmaf(ps, y, 3.1415926535897932385f);
+    sn = u * ps;
+    float pc = 2.3533063035889320454e-01f;
+    pc = fmaf(pc, y, -1.3352627688545894959f);
+    pc = fmaf(pc, y, 4.0587121264167682182f);
+    pc = fmaf(pc, y, -4.9348022005446793094f);
+    cs = fmaf(pc, y, 1.0f);
+}
+
+// q = n / d, r = n - q d for 0 <= n < 2^24, 1 <= d: float reciprocal, then an exact
+// fix-up of the (at most a few units) rounding error.
+__device__ __forceinline__ void divmod_small(int n, int d, float rd, int &q, int &r) {
+    q = (int)((float)n * rd);
+    r = n - q * d;
+    while (r < 0) { q -= 1; r += d; }
+    while (r >= d) { q += 1; r -= d; }
+}
+
+// sin(pi f), cos(pi f) for 0 <= f <= 1: sin as sinpi_unit, cos(pi f) = +-cos(pi g) by
+// the Taylor series of cos(pi g) through g^16 (remainder < 1e-12), g = min(f, 1 - f).
+__device__ __forceinline__ void sincospi_unit(float f, float &sn, float &cs) {
+    const bool upper = f > 0.5f;
+    const float g = upper ? 1.0f - f : f;
+    const float y = g * g;
+    float ps = -2.1915353447830215827e-05f;
+    ps = fmaf(ps, y, 4.6630280576761256442e-04f);
+    ps = fmaf(ps, y, -7.3704309457143507773e-03f);
+    ps = fmaf(ps, y, 8.2145886611128228799e-02f);
+    ps = fmaf(ps, y, -5.9926452932079207689e-01f);
+    ps = fmaf(ps, y, 2.5501640398773454439f);
+    ps = fmaf(ps, y, -5.1677127800499700292f);
+    ps = fmaf(ps, y, 3.1415926535897932385f);
+    sn = g * ps;
+    float pc = 4.3030695870329470073e-06f;
+    pc = fmaf(pc, y, -1.0463810492484570712e-04f);
+    pc = fmaf(pc, y, 1.9295743094039230479e-03f);
+    pc = fmaf(pc, y, -2.5806891390014060013e-02f);
+    pc = fmaf(pc, y, 2.3533063035889320454e-01f);
+    pc = fmaf(pc, y, -1.3352627688545894959f);
+    pc = fmaf(pc, y, 4.0587121264167682182f);
+    pc = fmaf(pc, y, -4.9348022005446793094f);
+    pc = fmaf(pc, y, 1.0f);
+    cs = upper ? -pc : pc;
+}
+
+// Distance from a float-float squared distance: an approximate square root s0
+// (rsqrt) and one Newton step s0 + (d2 - s0^2) / (2 s0), the residual by FMA exact to
+// ~1e-14 of d2.  inv_d is 1/distance to ~1e-7 (one Newton step on rsqrt).
+__device__ __forceinline__ ff ff_dist_newton(ff d2, float rs0, float s0, float &inv_d) {
+    const float rs = rs0 * fmaf(-0.5f * d2.hi * rs0, rs0, 1.5f);
+    const float res = fmaf(-s0, s0, d2.hi) + d2.lo;
+    inv_d = rs;
+    return ff_fast_two_sum(s0, 0.5f * res * rs);
+}
+
+// ---------------------------------------------------------------------------
 // Image bookkeeping of src/gpuRIR_cuda.cu:336-342: k = n - N/2,
 // clust = ceil(k/2), refl = |k mod 2|; coordinate 2*clust*L + (1-2 refl)*src.
 // ---------------------------------------------------------------------------

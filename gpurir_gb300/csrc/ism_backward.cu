@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
         const int N0 = R.nb[0], N1 = R.nb[1], N2 = R.nb[2];
         const int n_img = R.n_img;
         const float H = R.H, inv_h = 1.0f / H;
+        const float rN1 = 1.0f / (float)N1, rN2 = 1.0f / (float)N2;
+        const bool small_phi = inv_h <= 0.0625f;   // window angle f / H <= 1/16: series
         const int k_lo = (int)floorf(-H) + 1;
         const int spkr = R.spkr, mic = R.mic;
         const ff kfs = {R.kh, R.kl};
@@ -149,7 +151,9 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                 rn0[r] = 0;
                 ridx[r] = i;
                 if (i < n_img) {
-                    const int q = i / N2, m2 = i - q * N2, m0 = q / N1, m1 = q - m0 * N1;
+                    int q, m2, m0, m1;
+                    divmod_small(i, N2, rN2, q, m2);
+                    divmod_small(q, N1, rN1, m0, m1);
                     int c0, r0, c1, r1, c2, r2;
                     image_axis(m0, N0, c0, r0);
                     image_axis(m1, N1, c1, r1);
@@ -158,7 +162,15 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                     const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
                     const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
                     const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
-                    const ff tau = ff_mul(ff_sqrt(d2), kfs);
+                    // approximate distance first: far images stop here
+                    const float rs0 = rsqrtf(d2.hi);
+                    const float s0 = d2.hi * rs0;
+                    const float tau_est = s0 * kfs.hi;
+                    ff tau = {-1e30f, 0.0f};   // culled: fails the keep test below
+                    if (tau_est > keep_lo - 1.0f && tau_est < keep_hi + 1.0f) {
+                        float inv_d;
+                        tau = ff_mul(ff_dist_newton(d2, rs0, s0, inv_d), kfs);
+                    }
                     if (tau.hi > keep_lo && tau.hi < keep_hi) {
                         float fl = floorf(tau.hi);
                         int n0 = (int)fl;
@@ -167,8 +179,9 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                         if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
                         f = fmaxf(f, 9.094947017729282e-13f);
                         float sp, cp, sphi, cphi;
-                        sincospif(f, &sp, &cp);
-                        sincospif(f * inv_h, &sphi, &cphi);
+                        sincospi_unit(f, sp, cp);
+                        if (small_phi) sincospi_small(f * inv_h, sphi, cphi);
+                        else sincospif(f * inv_h, &sphi, &cphi);
                         r4[r] = make_float4(-sp * 0.318309886183790672f, f, cphi, sphi);
                         rg[r] = cp;
                         rn0[r] = n0 - t_lo;
@@ -262,7 +275,9 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
             // ---- pass C: chain rule, one kept image per lane
             for (int j = tid; j < n_kept; j += kBThreads) {
                 const int i = rec_idx[j];
-                const int q = i / N2, m2 = i - q * N2, m0 = q / N1, m1 = q - m0 * N1;
+                int q, m2, m0, m1;
+                divmod_small(i, N2, rN2, q, m2);
+                divmod_small(q, N1, rN1, m0, m1);
                 int cc[3], rr[3];
                 image_axis(m0, N0, cc[0], rr[0]);
                 image_axis(m1, N1, cc[1], rr[1]);

@@ -80,48 +80,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
-// sin(pi f) for 0 <= f <= 1: reflected to g = min(f, 1 - f) <= 1/2 (1 - f is exact
-// there), then the Taylor series of sin(pi g) = g * sum_k (-1)^k pi^(2k+1) g^(2k) / (2k+1)!
-// through k = 7 (remainder < 1e-9 relative), Horner in g^2.
-__device__ __forceinline__ float sinpi_unit(float f) {
-    const float g = fminf(f, 1.0f - f);
-    const float y = g * g;
-    float p = -2.1915353447830215827e-05f;
-    p = fmaf(p, y, 4.6630280576761256442e-04f);
-    p = fmaf(p, y, -7.3704309457143507773e-03f);
-    p = fmaf(p, y, 8.2145886611128228799e-02f);
-    p = fmaf(p, y, -5.9926452932079207689e-01f);
-    p = fmaf(p, y, 2.5501640398773454439f);
-    p = fmaf(p, y, -5.1677127800499700292f);
-    p = fmaf(p, y, 3.1415926535897932385f);
-    return g * p;
-}
-
-// sin(pi u), cos(pi u) for 0 <= u <= 1/16 by their Taylor series (remainders below
-// 1e-12 absolute): the per-image window angle, u = f / H.
-__device__ __forceinline__ void sincospi_small(float u, float &sn, float &cs) {
-    const float y = u * u;
-    float ps = -5.9926452932079207689e-01f;
-    ps = fmaf(ps, y, 2.5501640398773454439f);
-    ps = fmaf(ps, y, -5.1677127800499700292f);
-    ps = fmaf(ps, y, 3.1415926535897932385f);
-    sn = u * ps;
-    float pc = 2.3533063035889320454e-01f;
-    pc = fmaf(pc, y, -1.3352627688545894959f);
-    pc = fmaf(pc, y, 4.0587121264167682182f);
-    pc = fmaf(pc, y, -4.9348022005446793094f);
-    cs = fmaf(pc, y, 1.0f);
-}
-
-// q = n / d, r = n - q d for 0 <= n < 2^24, 1 <= d: float reciprocal, then an exact
-// fix-up of the (at most a few units) rounding error.
-__device__ __forceinline__ void divmod_small(int n, int d, float rd, int &q, int &r) {
-    q = (int)((float)n * rd);
-    r = n - q * d;
-    while (r < 0) { q -= 1; r += d; }
-    while (r >= d) { q += 1; r -= d; }
-}
-
 // Taps of one image into its sub-range buffer: lane l owns taps
 // k = k_lo + l + 32 i, i < TPL, at p[32 i].  With x = k - f the Hann window is
 //   0.5 (1 + cos(2 pi x / Tw)) = 0.5 + [0.5 cos(2 pi k/Tw)] cos(phi) + [0.5 sin(2 pi k/Tw)] sin(phi),
@@ -322,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             // ---- pass 1: geometry of this warp's images, per-warp histogram
             for (int s = lane; s < nsub; s += 32) my_hist[s] = 0;
             __syncwarp();
-#pragma unroll 1
+#pragma unroll 2
             for (int r = 0; r < kRounds; r++) {
                 const int local = warp * kPerWarp + r * 32 + lane;
                 const int i = cbase + local;
@@ -353,11 +311,9 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                                           __ldg(&R.pw[4][abs(c2 - r2)]) * __ldg(&R.pw[5][abs(c2)]);
                         // distance = s0 + (d2 - s0^2) / (2 s0): one Newton step in float-float
                         // (the residual by FMA is exact to ~1e-14 of d2)
-                        const float rs = rs0 * fmaf(-0.5f * d2.hi * rs0, rs0, 1.5f);   // 1/dist
-                        const float res = fmaf(-s0, s0, d2.hi) + d2.lo;
-                        const ff dist = ff_fast_two_sum(s0, 0.5f * res * rs);
+                        float inv_d;
+                        const ff dist = ff_dist_newton(d2, rs0, s0, inv_d);
                         const ff tau = ff_mul(dist, kfs);
-                        const float inv_d = rs;
                         float amp = att * (0.0795774715459476679f * inv_d);   // 1/(4 pi dist)
                         if (spkr != P_OMNI) {
                             // doa = image -> receiver = -vec; axis mirrored per reflection (:357-362)
