@@ -86,6 +86,10 @@ SIGNATURES.update({
                                             c_void_p, c_void_p]),
     "gpurir_ism_backward_batch_device": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,
                                                  c_float] + [c_void_p] * 11),
+    "gpurir_simulate_batch_device_beta": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float]
+                                          + [c_void_p] * 7),
+    "gpurir_ism_backward_batch_device_beta": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,
+                                                      c_float] + [c_void_p] * 12),
 })
 
 

@@ -9,6 +9,9 @@ if any, is produced by the forward pass but not differentiated.
     rirs = simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv)   # packed, autograd
     loss = ((rirs - target) ** 2).sum(); loss.backward()
 
+    model = TorchBatch(rooms, fs)            # structure prepared once for a training loop
+    rirs = model(beta, pos_src, pos_rcv)
+
 ``rooms`` fixes the static structure (room_sz, nb_img, Tmax, Tdiff, patterns
 and the per-room source/receiver counts); beta [n_rooms, 6], pos_src
 [sum n_src, 3], pos_rcv [sum n_rcv, 3] and the optional orientations are
@@ -26,53 +29,69 @@ from .batch import _room_struct, layout
 class _IsmBatch(torch.autograd.Function):
     @staticmethod
     def forward(ctx, beta, pos_src, pos_rcv, orV_src, orV_rcv, spec):
-        rooms, fs, c, sim = spec
-        rooms = [dict(r, beta=b) for r, b in zip(rooms, beta.detach().cpu().numpy())]
-        table = _room_struct(rooms)
-        off = layout(rooms, fs)
-        out = torch.empty(int(off[-1]), dtype=torch.float32, device=pos_src.device)
+        table, n_rooms, total, fs, c, sim = spec
+        out = torch.empty(total, dtype=torch.float32, device=pos_src.device)
         st = torch.cuda.current_stream(pos_src.device).cuda_stream
-        L = _lib.load()
         ptr = lambda t: t.data_ptr() if t is not None else None
-        _lib.check(L.gpurir_simulate_batch_device(sim.handle, len(rooms), table, float(fs), float(c),
-                                                  ptr(pos_src), ptr(pos_rcv), ptr(orV_src),
-                                                  ptr(orV_rcv), out.data_ptr(), ctypes.c_void_p(st)),
-                   "gpurir_simulate_batch_device")
-        ctx.spec = (rooms, fs, c, sim, table)
-        ctx.save_for_backward(pos_src, pos_rcv, orV_src, orV_rcv)
+        # beta stays on the device: the room tables are refreshed from it by a kernel
+        _lib.check(_lib.load().gpurir_simulate_batch_device_beta(
+            sim.handle, n_rooms, table, float(fs), float(c), beta.data_ptr(), ptr(pos_src), ptr(pos_rcv),
+            ptr(orV_src), ptr(orV_rcv), out.data_ptr(), ctypes.c_void_p(st)),
+            "gpurir_simulate_batch_device_beta")
+        ctx.spec = spec
+        ctx.save_for_backward(beta, pos_src, pos_rcv, orV_src, orV_rcv)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        rooms, fs, c, sim, table = ctx.spec
-        pos_src, pos_rcv, orV_src, orV_rcv = ctx.saved_tensors
+        table, n_rooms, total, fs, c, sim = ctx.spec
+        beta, pos_src, pos_rcv, orV_src, orV_rcv = ctx.saved_tensors
         g = grad_out.contiguous()
         dev = pos_src.device
-        gb = torch.empty((len(rooms), 6), dtype=torch.float32, device=dev) if ctx.needs_input_grad[0] else None
+        gb = torch.empty((n_rooms, 6), dtype=torch.float32, device=dev) if ctx.needs_input_grad[0] else None
         gs = torch.empty_like(pos_src) if ctx.needs_input_grad[1] else None
         gr = torch.empty_like(pos_rcv) if ctx.needs_input_grad[2] else None
         gos = torch.empty_like(orV_src) if orV_src is not None and ctx.needs_input_grad[3] else None
         gor = torch.empty_like(orV_rcv) if orV_rcv is not None and ctx.needs_input_grad[4] else None
         ptr = lambda t: t.data_ptr() if t is not None else None
         st = torch.cuda.current_stream(dev).cuda_stream
-        L = _lib.load()
-        _lib.check(L.gpurir_ism_backward_batch_device(
-            sim.handle, len(rooms), table, float(fs), float(c), ptr(pos_src), ptr(pos_rcv),
+        _lib.check(_lib.load().gpurir_ism_backward_batch_device_beta(
+            sim.handle, n_rooms, table, float(fs), float(c), beta.data_ptr(), ptr(pos_src), ptr(pos_rcv),
             ptr(orV_src), ptr(orV_rcv), g.data_ptr(), ptr(gb), ptr(gs), ptr(gr), ptr(gos), ptr(gor),
-            ctypes.c_void_p(st)), "gpurir_ism_backward_batch_device")
+            ctypes.c_void_p(st)), "gpurir_ism_backward_batch_device_beta")
         return gb, gs, gr, gos, gor, None
+
+
+class TorchBatch:
+    """The static structure of a batch (room sizes, image counts, lengths, patterns,
+    per-room source/receiver counts) prepared once; calling it with beta
+    [n_rooms, 6], positions and orientations (float32 CUDA tensors) returns the
+    packed RIRs with autograd through the early part.  Nothing of a step goes
+    through host memory, so a training loop can run back to back on the GPU."""
+
+    def __init__(self, rooms, fs, c=343.0, sim=None):
+        rooms = [dict(r, beta=r.get("beta", np.zeros(6, np.float32))) for r in rooms]
+        self.n_rooms = len(rooms)
+        self.table = _room_struct(rooms)
+        self.offsets = layout(rooms, fs)
+        self.fs, self.c = fs, c
+        self.sim = sim or simulator()
+
+    def __call__(self, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None):
+        for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv):
+            if t is not None and (t.dtype != torch.float32 or not t.is_cuda):
+                raise ValueError("beta, positions and orientations must be float32 CUDA tensors")
+        contig = lambda t: t.contiguous() if t is not None else None
+        spec = (self.table, self.n_rooms, int(self.offsets[-1]), self.fs, self.c, self.sim)
+        return _IsmBatch.apply(beta.reshape(self.n_rooms, 6).contiguous(), contig(pos_src), contig(pos_rcv),
+                               contig(orV_src), contig(orV_rcv), spec)
 
 
 def simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, c=343.0,
                          sim=None):
-    """Packed RIRs of a batch (float32 CUDA tensor) with autograd through the early part."""
-    for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv):
-        if t is not None and (t.dtype != torch.float32 or not t.is_cuda):
-            raise ValueError("beta, positions and orientations must be float32 CUDA tensors")
-    beta = beta.reshape(len(rooms), 6)
-    contig = lambda t: t.contiguous() if t is not None else None
-    return _IsmBatch.apply(beta, contig(pos_src), contig(pos_rcv), contig(orV_src), contig(orV_rcv),
-                           (rooms, fs, c, sim or simulator()))
+    """Packed RIRs of a batch (float32 CUDA tensor) with autograd through the early part
+    (prepares the batch structure on every call; TorchBatch keeps it)."""
+    return TorchBatch(rooms, fs, c, sim)(beta, pos_src, pos_rcv, orV_src, orV_rcv)
 
 
 def simulate_rir_torch(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,

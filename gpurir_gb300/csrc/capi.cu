@@ -53,6 +53,7 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
                             cudaStream_t st);
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
                        int L, long n_out, double *out, cudaStream_t st);
+cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
 }  // namespace gpurir
 
 using namespace gpurir;
@@ -526,7 +527,7 @@ static float *host_output_pointer(gpurir_sim *s, float *out) {
 static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, long n_rcv,
                           const float *pos_src, const float *pos_rcv, const float *orV_src,
                           const float *orV_rcv, float *out, long long out_elems, bool host_io,
-                          cudaStream_t st) {
+                          cudaStream_t st, const float *d_beta = nullptr) {
     Plan P;
     int rc = plan_rooms(s, R, P);
     if (rc) return rc;
@@ -553,6 +554,7 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     CK(cudaMemcpyAsync(d, h, L.stage_bytes, cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(s->stage_done, st));
     s->stage_pending = true;
+    if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(d + L.o_rooms), (int)R.size(), d_beta, st));
     float *dout = host_io ? reinterpret_cast<float *>(d + L.o_out) : out;
     // Host output the GPU can store to directly (pinned memory, or any host memory on
     // systems whose GPU shares the CPU's page tables, e.g. over NVLink-C2C): the kernels
@@ -728,10 +730,31 @@ extern "C" int gpurir_batch_layout(int n_rooms, const gpurir_room *rooms, float 
     return GPURIR_OK;
 }
 
+static int batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                        const float *d_beta, const float *d_pos_src, const float *d_pos_rcv,
+                        const float *d_orV_src, const float *d_orV_rcv, float *d_out, void *stream);
+
 extern "C" int gpurir_simulate_batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
                                             float Fs, float c, const float *d_pos_src,
                                             const float *d_pos_rcv, const float *d_orV_src,
                                             const float *d_orV_rcv, float *d_out, void *stream) {
+    return batch_device(s, n_rooms, rooms, Fs, c, nullptr, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
+                        d_out, stream);
+}
+
+extern "C" int gpurir_simulate_batch_device_beta(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
+                                                 float Fs, float c, const float *d_beta,
+                                                 const float *d_pos_src, const float *d_pos_rcv,
+                                                 const float *d_orV_src, const float *d_orV_rcv,
+                                                 float *d_out, void *stream) {
+    if (!d_beta) return fail(GPURIR_ERR_INVALID, "NULL d_beta");
+    return batch_device(s, n_rooms, rooms, Fs, c, d_beta, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
+                        d_out, stream);
+}
+
+static int batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                        const float *d_beta, const float *d_pos_src, const float *d_pos_rcv,
+                        const float *d_orV_src, const float *d_orV_rcv, float *d_out, void *stream) {
     if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
     if (!d_pos_src || !d_pos_rcv || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
     std::vector<RoomDesc> R;
@@ -743,7 +766,7 @@ extern "C" int gpurir_simulate_batch_device(gpurir_sim *s, int n_rooms, const gp
         if ((R[i].spkr != 0 && !d_orV_src) || (R[i].mic != 0 && !d_orV_rcv))
             return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
     return simulate_rooms(s, R, ns, nr, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_out, tot, false,
-                          reinterpret_cast<cudaStream_t>(stream));
+                          reinterpret_cast<cudaStream_t>(stream), d_beta);
 }
 
 // ---------------------------------------------------------------------------
@@ -875,6 +898,12 @@ static void csr(const std::vector<IsmItem> &items, int n_target, int IsmItem::*f
     for (size_t i = 0; i < items.size(); i++) list[fill[items[i].*field - base_sub]++] = (int)i;
 }
 
+static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                          const float *d_beta, const float *d_pos_src, const float *d_pos_rcv,
+                          const float *d_orV_src, const float *d_orV_rcv, const float *d_grad_rir,
+                          float *d_grad_beta, float *d_grad_pos_src, float *d_grad_pos_rcv,
+                          float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream);
+
 extern "C" int gpurir_ism_backward_batch_device(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
                                                 float Fs, float c, const float *d_pos_src,
                                                 const float *d_pos_rcv, const float *d_orV_src,
@@ -882,6 +911,30 @@ extern "C" int gpurir_ism_backward_batch_device(gpurir_sim *s, int n_rooms, cons
                                                 float *d_grad_beta, float *d_grad_pos_src,
                                                 float *d_grad_pos_rcv, float *d_grad_orV_src,
                                                 float *d_grad_orV_rcv, void *stream) {
+    return backward_batch(s, n_rooms, rooms, Fs, c, nullptr, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
+                          d_grad_rir, d_grad_beta, d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src,
+                          d_grad_orV_rcv, stream);
+}
+
+extern "C" int gpurir_ism_backward_batch_device_beta(gpurir_sim *s, int n_rooms, const gpurir_room *rooms,
+                                                     float Fs, float c, const float *d_beta,
+                                                     const float *d_pos_src, const float *d_pos_rcv,
+                                                     const float *d_orV_src, const float *d_orV_rcv,
+                                                     const float *d_grad_rir, float *d_grad_beta,
+                                                     float *d_grad_pos_src, float *d_grad_pos_rcv,
+                                                     float *d_grad_orV_src, float *d_grad_orV_rcv,
+                                                     void *stream) {
+    if (!d_beta) return fail(GPURIR_ERR_INVALID, "NULL d_beta");
+    return backward_batch(s, n_rooms, rooms, Fs, c, d_beta, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
+                          d_grad_rir, d_grad_beta, d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src,
+                          d_grad_orV_rcv, stream);
+}
+
+static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                          const float *d_beta, const float *d_pos_src, const float *d_pos_rcv,
+                          const float *d_orV_src, const float *d_orV_rcv, const float *d_grad_rir,
+                          float *d_grad_beta, float *d_grad_pos_src, float *d_grad_pos_rcv,
+                          float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream) {
     if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
     if (!d_pos_src || !d_pos_rcv || !d_grad_rir) return fail(GPURIR_ERR_INVALID, "NULL argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -924,6 +977,7 @@ extern "C" int gpurir_ism_backward_batch_device(gpurir_sim *s, int n_rooms, cons
     CK(cudaMemcpyAsync(d, h, stage_bytes, cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(s->stage_done, st));
     s->stage_pending = true;
+    if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(d + o_rooms), n_rooms, d_beta, st));
     float *ig = reinterpret_cast<float *>(d + o_ig);
     if (n_items == 0) {
         CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));

@@ -124,6 +124,15 @@ int gpurir_simulate_batch_device(gpurir_sim *sim, int n_rooms, const gpurir_room
                                  const float *d_orV_src, const float *d_orV_rcv, float *d_out,
                                  void *stream);
 
+/* As gpurir_simulate_batch_device, with the wall coefficients read on the device
+ * from d_beta [n_rooms][6] (the rooms' beta fields are not used): the power tables
+ * and Sabine T60 are refreshed by a kernel, so a differentiable step never copies
+ * beta to the host.  No counterpart in the reference. */
+int gpurir_simulate_batch_device_beta(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms, float Fs,
+                                      float c, const float *d_beta, const float *d_pos_src,
+                                      const float *d_pos_rcv, const float *d_orV_src,
+                                      const float *d_orV_rcv, float *d_out, void *stream);
+
 /* A batch planned once and captured in a CUDA graph.  gpurir_batch_launch
  * replays it on `stream`; positions/orientations are re-read from the device
  * buffers given at creation on every replay, and each replay draws the next
@@ -150,6 +159,16 @@ int gpurir_ism_backward_batch_device(gpurir_sim *sim, int n_rooms, const gpurir_
                                      float *d_grad_beta, float *d_grad_pos_src,
                                      float *d_grad_pos_rcv, float *d_grad_orV_src,
                                      float *d_grad_orV_rcv, void *stream);
+
+/* The adjoint with the wall coefficients read on the device from d_beta [n_rooms][6],
+ * as gpurir_simulate_batch_device_beta.  No counterpart in the reference. */
+int gpurir_ism_backward_batch_device_beta(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms,
+                                          float Fs, float c, const float *d_beta,
+                                          const float *d_pos_src, const float *d_pos_rcv,
+                                          const float *d_orV_src, const float *d_orV_rcv,
+                                          const float *d_grad_rir, float *d_grad_beta,
+                                          float *d_grad_pos_src, float *d_grad_pos_rcv,
+                                          float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream);
 
 /* Batched FFT convolutions of trajectory segments with their RIRs, host
  * buffers.  Replaces gpuRIR_cuda::cuda_convolutions, src/gpuRIR_cuda.cu:933-1023

@@ -171,3 +171,24 @@ def test_inverse_problem_recovers_walls(built):
         first = first if first is not None else float(loss.detach())
     assert float(loss.detach()) < 0.05 * first
     assert float((beta - true).abs().max()) < float((0.8 - true).abs().max())
+
+
+def test_device_beta_forward_matches_host_tables(built):
+    """TorchBatch refreshes the rooms' power tables from the device beta; the RIRs
+    agree with the batch entry that builds them on the host (FP64 pow there,
+    FP64 products here: float32-rounding level)."""
+    import torch
+    from gpurir_gb300 import batch as B
+    from gpurir_gb300.autograd import TorchBatch
+    from gpurir_gb300 import workloads
+    rooms = workloads.inverse_problem()[:4]
+    fs = 16000.0
+    host, _ = B.simulate_batch(rooms, fs)
+    dev = torch.device("cuda")
+    beta = torch.tensor(np.stack([r["beta"] for r in rooms]), device=dev)
+    ps = torch.tensor(np.concatenate([r["pos_src"] for r in rooms]), device=dev)
+    pr = torch.tensor(np.concatenate([r["pos_rcv"] for r in rooms]), device=dev)
+    orv = torch.tensor(np.concatenate([r["orV_rcv"] for r in rooms]), device=dev)
+    got = TorchBatch(rooms, fs)(beta, ps, pr, None, orv)
+    torch.cuda.synchronize()
+    assert rel_l2(got.cpu().numpy(), host.cpu().numpy()) < 1e-6
