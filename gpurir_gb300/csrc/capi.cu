@@ -84,6 +84,13 @@ struct gpurir_sim {
     cudaStream_t stream = nullptr;
     char *d_ws = nullptr;
     size_t d_ws_bytes = 0;
+    // Pinned staging of descriptors, a ring of kStageRing buffers so that a call never
+    // waits for the previous call's upload: h_stage / stage_done / stage_pending are
+    // the slot in use (ensure_stage rotates).
+    struct StageSlot { char *h = nullptr; size_t bytes = 0; cudaEvent_t ev = nullptr; bool pending = false; };
+    static constexpr int kStageRing = 4;
+    StageSlot stage_ring[kStageRing];
+    int stage_slot = 0;
     char *h_stage = nullptr;
     size_t h_stage_bytes = 0;
     cudaEvent_t stage_done = nullptr;
@@ -130,7 +137,9 @@ extern "C" int gpurir_create(int mixed_precision, int lookup_table, uint64_t see
     cudaError_t e = cudaGetDevice(&s->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->stage_done, cudaEventDisableTiming);
+    for (int k = 0; k < gpurir_sim::kStageRing && e == cudaSuccess; k++)
+        e = cudaEventCreateWithFlags(&s->stage_ring[k].ev, cudaEventDisableTiming);
+    s->stage_done = s->stage_ring[0].ev;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ws_busy, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->conv_busy, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_ctl, 4 * sizeof(int));
@@ -152,10 +161,13 @@ extern "C" int gpurir_destroy(gpurir_sim *s) {
     if (!s) return GPURIR_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->d_ws) cudaFree(s->d_ws);
-    if (s->h_stage) cudaFreeHost(s->h_stage);
+    s->stage_ring[s->stage_slot].h = s->h_stage;
+    for (int k = 0; k < gpurir_sim::kStageRing; k++)
+        if (s->stage_ring[k].h) cudaFreeHost(s->stage_ring[k].h);
     if (s->d_ctl) cudaFree(s->d_ctl);
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
-    if (s->stage_done) cudaEventDestroy(s->stage_done);
+    for (int k = 0; k < gpurir_sim::kStageRing; k++)
+        if (s->stage_ring[k].ev) cudaEventDestroy(s->stage_ring[k].ev);
     if (s->ws_busy) cudaEventDestroy(s->ws_busy);
     if (s->conv_busy) cudaEventDestroy(s->conv_busy);
     for (auto &t : s->twiddles) cudaFree(t.second);
@@ -283,9 +295,16 @@ static int build_room(RoomDesc &R, const float room[3], const float beta[6], con
     R.fs = Fs;
     R.pow_n = pow_table_len(nb);
     if (R.pow_n > kPowMax) return fail(GPURIR_ERR_INVALID, "nb_img too large for the reflection tables");
-    for (int w = 0; w < 6; w++)
-        for (int k = 0; k < kPowMax; k++)
-            R.pw[w][k] = k < R.pow_n ? (float)std::pow(-(double)beta[w], (double)k) : 0.0f;
+    // (-beta)^k by repeated FP64 products rounded to float32: the room-table kernel of
+    // the device-beta entries forms them the same way, so both paths agree bit for bit
+    for (int w = 0; w < 6; w++) {
+        const double m = -(double)beta[w];
+        double p = 1.0;
+        for (int k = 0; k < kPowMax; k++) {
+            R.pw[w][k] = k < R.pow_n ? (float)p : 0.0f;
+            p *= m;
+        }
+    }
     return GPURIR_OK;
 }
 
@@ -305,17 +324,29 @@ static int ensure_device(gpurir_sim *s, size_t bytes) {
 }
 
 static int ensure_stage(gpurir_sim *s, size_t bytes) {
-    if (s->stage_pending) {
-        CK(cudaEventSynchronize(s->stage_done));
-        s->stage_pending = false;
+    // park the slot in use, take the next one (its upload was issued kStageRing calls ago)
+    gpurir_sim::StageSlot &cur = s->stage_ring[s->stage_slot];
+    cur.h = s->h_stage;
+    cur.bytes = s->h_stage_bytes;
+    cur.pending = s->stage_pending;
+    s->stage_slot = (s->stage_slot + 1) % gpurir_sim::kStageRing;
+    gpurir_sim::StageSlot &g = s->stage_ring[s->stage_slot];
+    if (g.pending) {
+        CK(cudaEventSynchronize(g.ev));
+        g.pending = false;
     }
-    if (bytes <= s->h_stage_bytes) return GPURIR_OK;
-    if (s->h_stage) CK(cudaFreeHost(s->h_stage));
-    s->h_stage = nullptr;
-    s->h_stage_bytes = 0;
-    size_t want = align_up(bytes + bytes / 4, 1 << 16);
-    CK(cudaMallocHost(&s->h_stage, want));
-    s->h_stage_bytes = want;
+    if (bytes > g.bytes) {
+        if (g.h) CK(cudaFreeHost(g.h));
+        g.h = nullptr;
+        g.bytes = 0;
+        size_t want = align_up(bytes + bytes / 4, 1 << 16);
+        CK(cudaMallocHost(&g.h, want));
+        g.bytes = want;
+    }
+    s->h_stage = g.h;
+    s->h_stage_bytes = g.bytes;
+    s->stage_done = g.ev;
+    s->stage_pending = false;
     return GPURIR_OK;
 }
 

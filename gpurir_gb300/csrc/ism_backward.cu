@@ -399,9 +399,13 @@ size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
 
 template <int TPL>
 static cudaError_t bwd_tpl(const BwdLaunch &p, int grid, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(ism_backward_kernel<TPL>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
+    static bool attr_set = false;   // per process; the attribute is per function
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(ism_backward_kernel<TPL>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     ism_backward_kernel<TPL><<<grid, kBThreads, smem, st>>>(p);
     return cudaGetLastError();
 }

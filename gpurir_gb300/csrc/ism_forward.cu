@@ -24,6 +24,9 @@
 // constants and a per-image (cos, sin) pair (image_sample, :116-121).
 #include <cuda_fp16.h>
 
+#include <map>
+#include <mutex>
+
 #include "gpurir_internal.cuh"
 #include "tail_common.cuh"
 
@@ -607,7 +610,7 @@ static cudaError_t launch_tpl(const IsmLaunch &p, int grid, size_t smem, cudaStr
 }
 
 template <int MODE>
-static int occupancy(int tpl, size_t smem) {
+static int occupancy_query(int tpl, size_t smem) {
     int n = 0;
     switch (tpl) {
 #define OCC(T) case T: cudaFuncSetAttribute(ism_forward_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
@@ -616,6 +619,21 @@ static int occupancy(int tpl, size_t smem) {
 #undef OCC
     default: return 0;
     }
+    return n;
+}
+
+// Occupancy per (mode, taps per lane, shared memory), queried once: the queries cost
+// tens of microseconds, which small launches would pay on every call.
+template <int MODE>
+static int occupancy(int tpl, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::pair<int, size_t>, int> known;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(tpl, smem);
+    auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    const int n = occupancy_query<MODE>(tpl, smem);
+    known[key] = n;
     return n;
 }
 

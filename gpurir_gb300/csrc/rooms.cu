@@ -5,8 +5,7 @@
 // Per room: beta, the Sabine T60 of src/gpuRIR_cuda.cu:123-130 in float32 (as the
 // reference and the host path evaluate it), and the power tables
 // pw[w][k] = (-beta_w)^k, k < pow_n, formed in FP64 by repeated multiplication and
-// rounded to float32 (the host path rounds pow() in FP64; the two agree to well
-// below float32 rounding for k < 96).
+// rounded to float32, exactly as the host builds them (the same bits).
 #include "gpurir_internal.cuh"
 
 namespace gpurir {
