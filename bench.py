@@ -263,8 +263,28 @@ def _extra_inverse(workloads, sim, flush, stream, fs, dev):
         fwd(); fwd_bwd()
     t_f = _timed(fwd, 20, stream, flush)
     t_fb = _timed(fwd_bwd, 20, stream, flush)
+    # the same step recorded once in a CUDA graph (our calls only enqueue kernels) and
+    # replayed: what the GPU spends on it without PyTorch's per-op host overhead
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            beta.grad = ps.grad = pr.grad = None
+            fwd_bwd()
+            fwd()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    g_f, g_fb = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g_f):
+        fwd()
+    beta.grad = ps.grad = pr.grad = None
+    with torch.cuda.graph(g_fb):
+        fwd_bwd()
+    t_gf = _timed(g_f.replay, 20, stream, flush)
+    t_gfb = _timed(g_fb.replay, 20, stream, flush)
     out["inverse_problem"] = {"rirs": 16 * 32, "forward_ms": t_f, "forward_adjoint_ms": t_fb,
                               "adjoint_over_forward": t_fb / t_f,
+                              "graph_forward_ms": t_gf, "graph_forward_adjoint_ms": t_gfb,
+                              "graph_adjoint_over_forward": t_gfb / t_gf,
                               "note": "grads of an L2 loss w.r.t. beta[16,6], pos_src[64,3], "
                                       "pos_rcv[128,3]; beta stays on the device (TorchBatch)"}
     return out

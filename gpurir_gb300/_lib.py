@@ -86,6 +86,12 @@ SIGNATURES.update({
                                             c_void_p, c_void_p]),
     "gpurir_ism_backward_batch_device": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,
                                                  c_float] + [c_void_p] * 11),
+    "gpurir_adjoint_create": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float,
+                                      ctypes.POINTER(c_void_p)]),
+    "gpurir_adjoint_forward": (c_int, [c_void_p] * 8),
+    "gpurir_adjoint_backward": (c_int, [c_void_p] * 13),
+    "gpurir_adjoint_status": (c_int, [c_void_p, iptr]),
+    "gpurir_adjoint_destroy": (c_int, [c_void_p]),
     "gpurir_simulate_batch_device_beta": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float]
                                           + [c_void_p] * 7),
     "gpurir_ism_backward_batch_device_beta": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float,

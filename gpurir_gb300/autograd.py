@@ -28,63 +28,79 @@ from .batch import _room_struct, layout
 
 class _IsmBatch(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, beta, pos_src, pos_rcv, orV_src, orV_rcv, spec):
-        table, n_rooms, total, fs, c, sim = spec
-        out = torch.empty(total, dtype=torch.float32, device=pos_src.device)
+    def forward(ctx, beta, pos_src, pos_rcv, orV_src, orV_rcv, batch):
+        out = torch.empty(batch.total, dtype=torch.float32, device=pos_src.device)
         st = torch.cuda.current_stream(pos_src.device).cuda_stream
         ptr = lambda t: t.data_ptr() if t is not None else None
-        # beta stays on the device: the room tables are refreshed from it by a kernel
-        _lib.check(_lib.load().gpurir_simulate_batch_device_beta(
-            sim.handle, n_rooms, table, float(fs), float(c), beta.data_ptr(), ptr(pos_src), ptr(pos_rcv),
-            ptr(orV_src), ptr(orV_rcv), out.data_ptr(), ctypes.c_void_p(st)),
-            "gpurir_simulate_batch_device_beta")
-        ctx.spec = spec
+        # enqueue only: beta stays on the device, descriptors were uploaded at creation
+        _lib.check(_lib.load().gpurir_adjoint_forward(
+            batch.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
+            out.data_ptr(), ctypes.c_void_p(st)), "gpurir_adjoint_forward")
+        ctx.batch = batch
         ctx.save_for_backward(beta, pos_src, pos_rcv, orV_src, orV_rcv)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        table, n_rooms, total, fs, c, sim = ctx.spec
+        batch = ctx.batch
         beta, pos_src, pos_rcv, orV_src, orV_rcv = ctx.saved_tensors
         g = grad_out.contiguous()
         dev = pos_src.device
-        gb = torch.empty((n_rooms, 6), dtype=torch.float32, device=dev) if ctx.needs_input_grad[0] else None
+        gb = torch.empty((batch.n_rooms, 6), dtype=torch.float32, device=dev) if ctx.needs_input_grad[0] else None
         gs = torch.empty_like(pos_src) if ctx.needs_input_grad[1] else None
         gr = torch.empty_like(pos_rcv) if ctx.needs_input_grad[2] else None
         gos = torch.empty_like(orV_src) if orV_src is not None and ctx.needs_input_grad[3] else None
         gor = torch.empty_like(orV_rcv) if orV_rcv is not None and ctx.needs_input_grad[4] else None
         ptr = lambda t: t.data_ptr() if t is not None else None
         st = torch.cuda.current_stream(dev).cuda_stream
-        _lib.check(_lib.load().gpurir_ism_backward_batch_device_beta(
-            sim.handle, n_rooms, table, float(fs), float(c), beta.data_ptr(), ptr(pos_src), ptr(pos_rcv),
-            ptr(orV_src), ptr(orV_rcv), g.data_ptr(), ptr(gb), ptr(gs), ptr(gr), ptr(gos), ptr(gor),
-            ctypes.c_void_p(st)), "gpurir_ism_backward_batch_device_beta")
+        _lib.check(_lib.load().gpurir_adjoint_backward(
+            batch.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
+            g.data_ptr(), ptr(gb), ptr(gs), ptr(gr), ptr(gos), ptr(gor), ctypes.c_void_p(st)),
+            "gpurir_adjoint_backward")
         return gb, gs, gr, gos, gor, None
 
 
 class TorchBatch:
     """The static structure of a batch (room sizes, image counts, lengths, patterns,
-    per-room source/receiver counts) prepared once; calling it with beta
-    [n_rooms, 6], positions and orientations (float32 CUDA tensors) returns the
-    packed RIRs with autograd through the early part.  Nothing of a step goes
-    through host memory, so a training loop can run back to back on the GPU."""
+    per-room source/receiver counts) prepared once on the device (gpurir_adjoint);
+    calling it with beta [n_rooms, 6], positions and orientations (float32 CUDA
+    tensors) returns the packed RIRs with autograd through the early part.  A call
+    only enqueues kernels: nothing goes through host memory and nothing waits, so a
+    training step can run back to back or be recorded in a CUDA graph
+    (torch.cuda.graph)."""
 
     def __init__(self, rooms, fs, c=343.0, sim=None):
         rooms = [dict(r, beta=r.get("beta", np.zeros(6, np.float32))) for r in rooms]
         self.n_rooms = len(rooms)
-        self.table = _room_struct(rooms)
         self.offsets = layout(rooms, fs)
+        self.total = int(self.offsets[-1])
         self.fs, self.c = fs, c
         self.sim = sim or simulator()
+        self._L = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._L.gpurir_adjoint_create(self.sim.handle, self.n_rooms, _room_struct(rooms),
+                                                 float(fs), float(c), ctypes.byref(h)), "gpurir_adjoint_create")
+        self.handle = h
+
+    def __del__(self):
+        L, h = getattr(self, "_L", None), getattr(self, "handle", None)
+        if L is not None and h:
+            L.gpurir_adjoint_destroy(h)
+            self.handle = None
+
+    def status(self):
+        """Error word of the kernels (0: none); waits for them."""
+        v = ctypes.c_int()
+        _lib.check(self._L.gpurir_adjoint_status(self.handle, ctypes.byref(v)), "gpurir_adjoint_status")
+        return v.value
 
     def __call__(self, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None):
         for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv):
             if t is not None and (t.dtype != torch.float32 or not t.is_cuda):
                 raise ValueError("beta, positions and orientations must be float32 CUDA tensors")
         contig = lambda t: t.contiguous() if t is not None else None
-        spec = (self.table, self.n_rooms, int(self.offsets[-1]), self.fs, self.c, self.sim)
         return _IsmBatch.apply(beta.reshape(self.n_rooms, 6).contiguous(), contig(pos_src), contig(pos_rcv),
-                               contig(orV_src), contig(orV_rcv), spec)
+                               contig(orV_src), contig(orV_rcv), self)
 
 
 def simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, c=343.0,

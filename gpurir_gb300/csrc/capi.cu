@@ -39,7 +39,7 @@ size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad);
 cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                 const float *pos_src, const float *pos_rcv, const float *orv_src,
                                 const float *orv_rcv, const float *grad, float *item_grad,
-                                int *work_counter, int *status, int max_tseg, int grid,
+                                int *work_counter, int *status, int max_tseg, int grid, int clamp,
                                 cudaStream_t st);
 cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
                                int comp_lo, int n_comp, float *out, cudaStream_t st);
@@ -1020,7 +1020,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
         CK(ism_backward_launch(P.tpl, reinterpret_cast<const RoomDesc *>(d + o_rooms),
                                reinterpret_cast<const IsmItem *>(d + o_items), n_items, d_pos_src,
                                d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, s->d_ctl, s->d_ctl + 1,
-                               max_tseg, grid, st));
+                               max_tseg, grid, P.clamp, st));
     }
     const int *dp[6];
     for (int a = 0; a < 6; a++) dp[a] = reinterpret_cast<const int *>(d + o_arr[a]);
@@ -1031,6 +1031,136 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     if (d_grad_orV_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)nr, 15, 3, d_grad_orV_rcv, st));
     CK(cudaEventRecord(s->ws_busy, st));
     s->ws_recorded = true;
+    return GPURIR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Training-loop batch: descriptors, work items and gradient lists uploaded once;
+// the forward and the adjoint then only enqueue kernels (no host work, no
+// synchronisation), so a whole step can be recorded in a CUDA graph.
+// ---------------------------------------------------------------------------
+struct gpurir_adjoint {
+    gpurir_sim *sim = nullptr;
+    char *d = nullptr;
+    Plan P;
+    Layout L;
+    int n_rooms = 0;
+    long ns = 0, nr = 0, M = 0;
+    long long out_elems = 0;
+    int max_tseg = 1, grid_b = 0;
+    bool need_orv_src = false, need_orv_rcv = false;
+    size_t o_arr[6] = {}, o_ig = 0, o_ctl = 0;
+};
+
+extern "C" int gpurir_adjoint_destroy(gpurir_adjoint *a) {
+    if (!a) return GPURIR_OK;
+    if (a->d) cudaFree(a->d);
+    delete a;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs,
+                                     float c, gpurir_adjoint **out) {
+    if (!s || !out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    gpurir_adjoint *a = new gpurir_adjoint();
+    a->sim = s;
+    a->n_rooms = n_rooms;
+    std::vector<RoomDesc> R;
+    int rc = build_batch(n_rooms, rooms, Fs, c, R, a->ns, a->nr, a->out_elems);
+    if (rc == GPURIR_OK) rc = plan_rooms(s, R, a->P);
+    if (rc) { delete a; return rc; }
+    for (const RoomDesc &r : R) {
+        a->need_orv_src |= r.spkr != 0;
+        a->need_orv_rcv |= r.mic != 0;
+    }
+    const Plan &P = a->P;
+    a->M = (long)P.rirs.size();
+    a->L = make_layout(P, R.size(), a->ns, a->nr, a->M, a->out_elems, false);
+    const int n_items = (int)P.items.size();
+    for (const IsmItem &it : P.items) a->max_tseg = std::max(a->max_tseg, it.t_hi - it.t_lo);
+    if (n_items > 0 && ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl) > 227 * 1024) {
+        delete a;
+        return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
+    }
+    a->grid_b = std::min(n_items, s->num_sms);
+    std::vector<int> lists[6];
+    csr(P.items, n_rooms, &IsmItem::room, 0, lists[0], lists[1]);
+    csr(P.items, (int)a->ns, &IsmItem::src, 0, lists[2], lists[3]);
+    csr(P.items, (int)a->nr, &IsmItem::rcv, 0, lists[4], lists[5]);
+    size_t off = align_up(a->L.o_out, 256);
+    for (int k = 0; k < 6; k++) { a->o_arr[k] = off; off = align_up(off + lists[k].size() * sizeof(int), 256); }
+    a->o_ig = off;
+    a->o_ctl = align_up(a->o_ig + (size_t)std::max(n_items, 1) * 18 * sizeof(float), 256);
+    const size_t bytes = a->o_ctl + 256;   // [0] forward counter, [1] adjoint counter, [2] status, +16 call offset
+    std::vector<char> h(a->o_ctl + 256, 0);
+    fill_stage(h.data(), a->L, R, P);
+    for (int k = 0; k < 6; k++)
+        if (!lists[k].empty()) memcpy(h.data() + a->o_arr[k], lists[k].data(), lists[k].size() * sizeof(int));
+    const uint64_t start = s->calls;
+    memcpy(h.data() + a->o_ctl + 16, &start, sizeof(start));
+    cudaError_t e = cudaMalloc(&a->d, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(a->d, h.data(), bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        gpurir_adjoint_destroy(a);
+        return fail(GPURIR_ERR_CUDA, std::string("gpurir_adjoint_create: ") + cudaGetErrorString(e));
+    }
+    *out = a;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_adjoint_forward(gpurir_adjoint *a, const float *d_beta, const float *d_pos_src,
+                                      const float *d_pos_rcv, const float *d_orV_src,
+                                      const float *d_orV_rcv, float *d_out, void *stream) {
+    if (!a || !d_beta || !d_pos_src || !d_pos_rcv || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if ((a->need_orv_src && !d_orV_src) || (a->need_orv_rcv && !d_orV_rcv))
+        return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int *ctl = reinterpret_cast<int *>(a->d + a->o_ctl);
+    uint64_t *offset = reinterpret_cast<uint64_t *>(a->d + a->o_ctl + 16);
+    CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
+    int rc = enqueue_kernels(a->sim, a->P, a->d, a->L, a->M, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
+                             d_out, ctl, offset, st, false);
+    if (rc) return rc;
+    if (a->P.max_n_diff > 0) CK(advance_counter_launch(offset, st));   // the next call draws new noise
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, const float *d_pos_src,
+                                       const float *d_pos_rcv, const float *d_orV_src,
+                                       const float *d_orV_rcv, const float *d_grad_rir, float *d_grad_beta,
+                                       float *d_grad_pos_src, float *d_grad_pos_rcv, float *d_grad_orV_src,
+                                       float *d_grad_orV_rcv, void *stream) {
+    if (!a || !d_beta || !d_pos_src || !d_pos_rcv || !d_grad_rir) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if ((a->need_orv_src && !d_orV_src) || (a->need_orv_rcv && !d_orV_rcv))
+        return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int *ctl = reinterpret_cast<int *>(a->d + a->o_ctl);
+    const Plan &P = a->P;
+    const int n_items = (int)P.items.size();
+    float *ig = reinterpret_cast<float *>(a->d + a->o_ig);
+    const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(a->d + a->L.o_rooms);
+    CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
+    if (n_items == 0) {
+        CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));
+    } else {
+        CK(ism_backward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(a->d + a->L.o_items), n_items,
+                               d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, ctl + 1, ctl + 2,
+                               a->max_tseg, a->grid_b, P.clamp, st));
+    }
+    const int *dp[6];
+    for (int k = 0; k < 6; k++) dp[k] = reinterpret_cast<const int *>(a->d + a->o_arr[k]);
+    if (d_grad_beta) CK(grad_reduce_launch(ig, dp[0], dp[1], a->n_rooms, 0, 6, d_grad_beta, st));
+    if (d_grad_pos_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)a->ns, 6, 3, d_grad_pos_src, st));
+    if (d_grad_pos_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)a->nr, 9, 3, d_grad_pos_rcv, st));
+    if (d_grad_orV_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)a->ns, 12, 3, d_grad_orV_src, st));
+    if (d_grad_orV_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)a->nr, 15, 3, d_grad_orV_rcv, st));
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_adjoint_status(gpurir_adjoint *a, int *status) {
+    if (!a || !status) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    CK(cudaMemcpy(status, a->d + a->o_ctl + 2 * sizeof(int), sizeof(int), cudaMemcpyDeviceToHost));
     return GPURIR_OK;
 }
 

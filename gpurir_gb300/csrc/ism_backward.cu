@@ -59,7 +59,7 @@ __device__ __forceinline__ float pattern_slope(int pattern) {
     }
 }
 
-template <int TPL>
+template <int TPL, bool CLAMP>
 __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P) {
     constexpr int KS = 32 * TPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
         const float fs_c = R.kh + R.kl;   // Fs / c
         const float dws = 3.14159265358979323846f * inv_h;   // 2 pi / Tw
         // per-lane tap constants
-        float kf[TPL], ck[TPL], sk[TPL];
+        float kf[TPL], ck[TPL], sk[TPL], ckd[TPL], skd[TPL];   // ckd, skd: times 2 pi / Tw
 #pragma unroll
         for (int i = 0; i < TPL; i++) {
             kf[i] = (float)(k_lo + lane + 32 * i);
@@ -128,6 +128,8 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
             sincospif(kf[i] * inv_h, &sn, &cs);
             ck[i] = 0.5f * cs;
             sk[i] = 0.5f * sn;
+            ckd[i] = dws * ck[i];
+            skd[i] = dws * sk[i];
         }
         const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
         float acc[kGrad];
@@ -242,11 +244,10 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                             const float x = kf[i] - f;
                             const float rx_ = rcp_approx_b(x);
                             const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
-                            const float wd = dws * fmaf(ck[i], sphi, -sk[i] * cphi);
+                            const float wd = fmaf(ckd[i], sphi, -skd[i] * cphi);
                             const float s = sig * rx_;
-                            const float sd = (gam - s) * rx_;
-                            float W = w * s, Wd = fmaf(wd, s, w * sd);
-                            if (fabsf(x) >= H) { W = 0.0f; Wd = 0.0f; }
+                            float W = w * s, Wd = fmaf(wd, s, w * ((gam - s) * rx_));
+                            if (CLAMP && fabsf(x) >= H) { W = 0.0f; Wd = 0.0f; }
                             const float g = gp[32 * i];
                             a[u] = fmaf(g, W, a[u]);
                             b[u] = fmaf(g, Wd, b[u]);
@@ -397,23 +398,23 @@ size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
            kBWarps * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
 }
 
-template <int TPL>
+template <int TPL, bool CLAMP>
 static cudaError_t bwd_tpl(const BwdLaunch &p, int grid, size_t smem, cudaStream_t st) {
     static bool attr_set = false;   // per process; the attribute is per function
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(ism_backward_kernel<TPL>,
+        cudaError_t e = cudaFuncSetAttribute(ism_backward_kernel<TPL, CLAMP>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    ism_backward_kernel<TPL><<<grid, kBThreads, smem, st>>>(p);
+    ism_backward_kernel<TPL, CLAMP><<<grid, kBThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                 const float *pos_src, const float *pos_rcv, const float *orv_src,
                                 const float *orv_rcv, const float *grad, float *item_grad,
-                                int *work_counter, int *status, int max_tseg, int grid,
+                                int *work_counter, int *status, int max_tseg, int grid, int clamp,
                                 cudaStream_t st) {
     BwdLaunch p;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
@@ -424,13 +425,20 @@ cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *i
     size_t smem = ism_backward_smem_bytes(tpl, max_tseg, p.pad);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    switch (tpl) {
-    case 2: return bwd_tpl<2>(p, grid, smem, st);
-    case 4: return bwd_tpl<4>(p, grid, smem, st);
-    case 8: return bwd_tpl<8>(p, grid, smem, st);
-    case 12: return bwd_tpl<12>(p, grid, smem, st);
-    case 16: return bwd_tpl<16>(p, grid, smem, st);
-    case 24: return bwd_tpl<24>(p, grid, smem, st);
+    // taps beyond |x| < Tw/2 exist only when the window does not fill the lanes exactly
+    switch (tpl * 2 + (clamp ? 1 : 0)) {
+    case 4: return bwd_tpl<2, false>(p, grid, smem, st);
+    case 5: return bwd_tpl<2, true>(p, grid, smem, st);
+    case 8: return bwd_tpl<4, false>(p, grid, smem, st);
+    case 9: return bwd_tpl<4, true>(p, grid, smem, st);
+    case 16: return bwd_tpl<8, false>(p, grid, smem, st);
+    case 17: return bwd_tpl<8, true>(p, grid, smem, st);
+    case 24: return bwd_tpl<12, false>(p, grid, smem, st);
+    case 25: return bwd_tpl<12, true>(p, grid, smem, st);
+    case 32: return bwd_tpl<16, false>(p, grid, smem, st);
+    case 33: return bwd_tpl<16, true>(p, grid, smem, st);
+    case 48: return bwd_tpl<24, false>(p, grid, smem, st);
+    case 49: return bwd_tpl<24, true>(p, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
 }

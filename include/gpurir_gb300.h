@@ -170,6 +170,28 @@ int gpurir_ism_backward_batch_device_beta(gpurir_sim *sim, int n_rooms, const gp
                                           float *d_grad_pos_src, float *d_grad_pos_rcv,
                                           float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream);
 
+/* A batch prepared once for training loops: room descriptors, work items and the
+ * gradient reduction lists are uploaded at creation; gpurir_adjoint_forward and
+ * gpurir_adjoint_backward then only enqueue kernels on `stream` (no host work, no
+ * synchronisation, no allocation), reading the wall coefficients from d_beta
+ * [n_rooms][6] at every call, so a whole step (forward, loss, adjoint) can be
+ * recorded in a CUDA graph.  Arguments as gpurir_simulate_batch_device_beta and
+ * gpurir_ism_backward_batch_device_beta.  gpurir_adjoint_status returns the
+ * kernels' error word (0: none).  No counterpart in the reference. */
+typedef struct gpurir_adjoint gpurir_adjoint;
+int gpurir_adjoint_create(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms, float Fs, float c,
+                          gpurir_adjoint **out);
+int gpurir_adjoint_forward(gpurir_adjoint *adj, const float *d_beta, const float *d_pos_src,
+                           const float *d_pos_rcv, const float *d_orV_src, const float *d_orV_rcv,
+                           float *d_out, void *stream);
+int gpurir_adjoint_backward(gpurir_adjoint *adj, const float *d_beta, const float *d_pos_src,
+                            const float *d_pos_rcv, const float *d_orV_src, const float *d_orV_rcv,
+                            const float *d_grad_rir, float *d_grad_beta, float *d_grad_pos_src,
+                            float *d_grad_pos_rcv, float *d_grad_orV_src, float *d_grad_orV_rcv,
+                            void *stream);
+int gpurir_adjoint_status(gpurir_adjoint *adj, int *status);
+int gpurir_adjoint_destroy(gpurir_adjoint *adj);
+
 /* Batched FFT convolutions of trajectory segments with their RIRs, host
  * buffers.  Replaces gpuRIR_cuda::cuda_convolutions, src/gpuRIR_cuda.cu:933-1023
  * (called by gpuRIR_bind::gpu_conv, src/python_bind.cpp:90-119), same argument

@@ -192,3 +192,44 @@ def test_device_beta_forward_matches_host_tables(built):
     got = TorchBatch(rooms, fs)(beta, ps, pr, None, orv)
     torch.cuda.synchronize()
     assert np.array_equal(got.cpu().numpy(), host.cpu().numpy())
+
+
+def test_training_step_in_a_cuda_graph(built):
+    """TorchBatch only enqueues kernels: forward, loss and adjoint record into one CUDA
+    graph, and replays give the eager step's gradients."""
+    import torch
+    from gpurir_gb300.autograd import TorchBatch
+    from gpurir_gb300 import workloads
+    rooms = workloads.inverse_problem()[:3]
+    fs = 16000.0
+    dev = torch.device("cuda")
+    model = TorchBatch(rooms, fs)
+    beta0 = np.stack([r["beta"] for r in rooms])
+    beta = torch.tensor(beta0, device=dev, requires_grad=True)
+    ps = torch.tensor(np.concatenate([r["pos_src"] for r in rooms]), device=dev, requires_grad=True)
+    pr = torch.tensor(np.concatenate([r["pos_rcv"] for r in rooms]), device=dev)
+    orv = torch.tensor(np.concatenate([r["orV_rcv"] for r in rooms]), device=dev)
+    target = model(beta.detach() * 0.98, ps.detach(), pr, None, orv).detach()
+
+    def step():
+        loss = ((model(beta, ps, pr, None, orv) - target) ** 2).sum()
+        loss.backward()
+
+    step()
+    eager = (beta.grad.clone(), ps.grad.clone())
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            beta.grad = ps.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    beta.grad = ps.grad = None
+    with torch.cuda.graph(graph):
+        step()
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(beta.grad, eager[0]) and torch.equal(ps.grad, eager[1])
+    assert model.status() == 0
