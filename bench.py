@@ -144,7 +144,7 @@ def run_reference(a):
     step_s = sum(times) / len(times)
     value = n_rir / step_s
     sample = "%d of 64 sources x 32 receivers (%d RIRs) per step, early part only" % (n_src, n_rir)
-    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "RIRs/s", "n_gpus": 0,
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "RIRs/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": {"workload": WORKLOAD_DESC},
@@ -153,8 +153,9 @@ def run_reference(a):
                              "sample": sample},
             "e2e": {"value": value, "unit": "RIRs/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the ISM path (OpenMP, FP32): the reference has no CPU "
-                    "implementation and its CUDA build cannot run in this environment"}
+            "note": "runs on the host cores: the reference has no CPU implementation of the path, "
+                    "so its FP32 restatement (OpenMP, windowed) is timed; gpuRIR's own CUDA kernels "
+                    "on the same GPU are timed by oracle/time_reference_kernels.py"}
     print(json.dumps(line), flush=True)
 
 
