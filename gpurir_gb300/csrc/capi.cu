@@ -27,7 +27,7 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw, const TailArgs *tail);
+                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
@@ -353,6 +353,7 @@ static int ensure_stage(gpurir_sim *s, size_t bytes) {
 struct Plan {
     int tpl, em, nsub, grid, clamp;
     long unfused_tails = 0;   // RIRs whose tail the separate tail kernel writes
+    int axis_cap = 0;         // per-axis table entries per block (max over rooms of N0 + N1 + N2)
     int mode = 0, tw = 0;   // tap evaluation mode (0 FP32, 1 mixed precision, 2 LUT), window length
     int max_n_diff;
     std::vector<IsmItem> items;
@@ -389,9 +390,11 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     const int sub = 32 * P.tpl;
     long M_tot = 0;
     P.max_n_diff = 0;
+    P.axis_cap = 0;
     for (const RoomDesc &r : R) {
         M_tot += (long)r.n_src * r.n_rcv;
         P.max_n_diff = std::max(P.max_n_diff, r.n_total - r.n_ism);
+        P.axis_cap = std::max(P.axis_cap, r.nb[0] + r.nb[1] + r.nb[2]);
     }
     P.items.clear();
     P.rirs.clear();
@@ -471,7 +474,7 @@ static int check_status(gpurir_sim *s) {
 
 // Byte layout of one launch's descriptors (mirrored host staging -> device).
 struct Layout {
-    size_t o_rooms, o_items, o_rirs, o_pos, stage_bytes, o_env, o_out, dev_bytes;
+    size_t o_rooms, o_items, o_rirs, o_pos, stage_bytes, o_env, o_axis, o_out, dev_bytes;
 };
 
 static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv, long M,
@@ -484,7 +487,8 @@ static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv,
     size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
     L.stage_bytes = align_up(L.o_pos + n_pos * sizeof(float), 256);
     L.o_env = L.stage_bytes;
-    L.o_out = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
+    L.o_axis = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
+    L.o_out = align_up(L.o_axis + (size_t)P.grid * P.axis_cap * sizeof(float4), 256);
     L.dev_bytes = L.o_out + (host_io ? (size_t)out_elems * sizeof(float) : 0);
     return L;
 }
@@ -513,7 +517,8 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
-                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw, &ta));
+                              s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw, &ta,
+                              reinterpret_cast<float4 *>(const_cast<char *>(d) + L.o_axis), P.axis_cap));
     if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
     const bool tail_kernel = P.max_n_diff > 0 && (P.unfused_tails > 0 || P.grid == 0);
     if (record && s->profile && tail_kernel) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }

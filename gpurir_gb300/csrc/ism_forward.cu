@@ -63,6 +63,11 @@ struct IsmLaunch {
     int noise_kind;
     float *env_out;
     int fuse_tail;
+    // per-axis image terms of the current item, one region of axis_cap entries per block
+    // (global memory, L1-resident): {v^2 hi, v^2 lo, v hi, attenuation} for m < N0, then
+    // N1, then N2 entries.  nullptr: computed per image instead.
+    float4 *axis_tab;
+    int axis_cap;
 };
 
 // Evaluation modes of the taps (template parameter MODE):
@@ -244,6 +249,27 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const float inv_h = 1.0f / H;
         const float rN1 = 1.0f / (float)N1, rN2 = 1.0f / (float)N2;
         const bool small_phi = inv_h <= 0.0625f;   // window angle f / H <= 1/16: polynomials
+        // per-axis terms once per item: an image's squared distance is then two
+        // float-float additions (the same operations, in the same order, as per image)
+        float4 *tab = P.axis_tab ? P.axis_tab + (size_t)blockIdx.x * P.axis_cap : nullptr;
+        const bool use_tab = tab && N0 + N1 + N2 <= P.axis_cap;
+        if (use_tab) {
+            for (int e = tid; e < N0 + N1 + N2; e += kThreads) {
+                const int a = e < N0 ? 0 : (e < N0 + N1 ? 1 : 2);
+                const int m = e - (a == 0 ? 0 : (a == 1 ? N0 : N0 + N1));
+                const int Na = a == 0 ? N0 : (a == 1 ? N1 : N2);
+                const float La = a == 0 ? L0 : (a == 1 ? L1 : L2);
+                const float sa = a == 0 ? P.pos_src[3 * it.src] : (a == 1 ? P.pos_src[3 * it.src + 1] : P.pos_src[3 * it.src + 2]);
+                const float ra = a == 0 ? P.pos_rcv[3 * it.rcv] : (a == 1 ? P.pos_rcv[3 * it.rcv + 1] : P.pos_rcv[3 * it.rcv + 2]);
+                int ca, fa;
+                image_axis(m, Na, ca, fa);
+                const ff v = ff_add(ff_two_prod((float)(2 * ca), La), ff_two_sum(fa ? -sa : sa, -ra));
+                const ff sq = ff_sqr(v);
+                const float att = R.pw[2 * a][abs(ca - fa)] * R.pw[2 * a + 1][abs(ca)];
+                tab[e] = make_float4(sq.hi, sq.lo, v.hi, att);
+            }
+            __syncthreads();
+        }
         const int k_lo = (int)floorf(-H) + 1;
         const int spkr = R.spkr, mic = R.mic;
         const ff kfs = {R.kh, R.kl};
@@ -299,17 +325,28 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     image_axis(m1, N1, c1, r1);
                     image_axis(m2, N2, c2, r2);
                     // vector receiver -> image, float-float (src/gpuRIR_cuda.cu:353)
-                    const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
-                    const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
-                    const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
-                    const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
+                    ff d2;
+                    float v0h, v1h, v2h, att_t = 0.0f;
+                    if (use_tab) {
+                        const float4 t0 = tab[m0], t1 = tab[N0 + m1], t2 = tab[N0 + N1 + m2];
+                        d2 = ff_add(ff_add(ff{t0.x, t0.y}, ff{t1.x, t1.y}), ff{t2.x, t2.y});
+                        v0h = t0.z; v1h = t1.z; v2h = t2.z;
+                        att_t = t0.w * t1.w * t2.w;
+                    } else {
+                        const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
+                        const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
+                        const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
+                        d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
+                        v0h = v0.hi; v1h = v1.hi; v2h = v2.hi;
+                    }
                     // approximate distance first: images whose delay is far outside this
                     // segment (a third of them in a room's corner regions) stop here
                     const float rs0 = rsqrtf(d2.hi);
                     const float s0 = d2.hi * rs0;
                     const float tau_est = s0 * kfs.hi;
                     if (tau_est > keep_lo - 1.0f && tau_est < keep_hi + 1.0f) {
-                        const float att = __ldg(&R.pw[0][abs(c0 - r0)]) * __ldg(&R.pw[1][abs(c0)]) *
+                        const float att = use_tab ? att_t :
+                                          __ldg(&R.pw[0][abs(c0 - r0)]) * __ldg(&R.pw[1][abs(c0)]) *
                                           __ldg(&R.pw[2][abs(c1 - r1)]) * __ldg(&R.pw[3][abs(c1)]) *
                                           __ldg(&R.pw[4][abs(c2 - r2)]) * __ldg(&R.pw[5][abs(c2)]);
                         // distance = s0 + (d2 - s0^2) / (2 s0): one Newton step in float-float
@@ -320,12 +357,12 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                         float amp = att * (0.0795774715459476679f * inv_d);   // 1/(4 pi dist)
                         if (spkr != P_OMNI) {
                             // doa = image -> receiver = -vec; axis mirrored per reflection (:357-362)
-                            float ct = -((r0 ? -os0 : os0) * v0.hi + (r1 ? -os1 : os1) * v1.hi +
-                                         (r2 ? -os2 : os2) * v2.hi) * inv_d;
+                            float ct = -((r0 ? -os0 : os0) * v0h + (r1 ? -os1 : os1) * v1h +
+                                         (r2 ? -os2 : os2) * v2h) * inv_d;
                             amp *= pattern_gain(ct, spkr);
                         }
                         if (mic != P_OMNI) {
-                            float ct = (or0 * v0.hi + or1 * v1.hi + or2 * v2.hi) * inv_d;   // (:363)
+                            float ct = (or0 * v0h + or1 * v1h + or2 * v2h) * inv_d;   // (:363)
                             amp *= pattern_gain(ct, mic);
                         }
                         float fl = floorf(tau.hi);
@@ -663,8 +700,10 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw, const TailArgs *tail) {
+                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap) {
     IsmLaunch p;
+    p.axis_tab = axis_tab;
+    p.axis_cap = axis_cap;
     p.seed = tail ? tail->seed : 0;
     p.offset = tail ? tail->offset : 0;
     p.offset_ptr = tail ? tail->offset_ptr : nullptr;
