@@ -305,7 +305,26 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const float lane_sign = (((k_lo + lane) & 1) ? -1.0f : 1.0f) * (MODE == kModeF32 ? 0.5f : 1.0f);
         int *my_hist = hist + warp * kMaxSub;
 
+        // Chunks whose rows (fixed m0, m1) all lie farther from the receiver than the
+        // segment's latest delay reaches, in the xy-plane alone, hold no image of the
+        // segment: skipped whole (a conservative test on the tables' leading parts).
+        const float d_hi = (keep_hi + 2.0f) / kfs.hi + 0.01f;
+        const float dhi2 = d_hi * d_hi;
+        // |component| <= (|k| + 1) L on each axis: when even the farthest row is within
+        // reach, nothing can be skipped and the test is not made
+        const float x_max = (float)(N0 / 2 + 1) * L0, y_max = (float)(N1 / 2 + 1) * L1;
+        const bool may_skip = use_tab && x_max * x_max + y_max * y_max > dhi2;
         for (int cbase = 0; cbase < n_img; cbase += kChunk) {
+            if (may_skip) {
+                const int q_first = cbase / N2, q_last = (min(cbase + kChunk, n_img) - 1) / N2;
+                int hit = 0;
+                for (int q = q_first + tid; q <= q_last && !hit; q += kThreads) {
+                    int m0, m1;
+                    divmod_small(q, N1, rN1, m0, m1);
+                    hit = tab[m0].x + tab[N0 + m1].x <= dhi2;
+                }
+                if (!__syncthreads_or(hit)) continue;
+            }
             // ---- pass 1: geometry of this warp's images, per-warp histogram
             for (int s = lane; s < nsub; s += 32) my_hist[s] = 0;
             __syncwarp();
