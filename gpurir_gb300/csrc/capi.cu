@@ -27,7 +27,10 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap);
+                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
+                               float *partial);
+cudaError_t partial_reduce_launch(const PartGroup *groups, int n_groups, int max_len, const float *part,
+                                  float *out, cudaStream_t st);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
@@ -75,6 +78,7 @@ static int fail(int code, const std::string &msg) {
 // Per-ISM-launch smem budget: two blocks of 512 threads per SM.
 static const size_t kSmemBudget = 113 * 1024;   // two blocks per SM (228 KB less 1 KB each)
 static const size_t kSmemBudgetLarge = 220 * 1024;
+static const long kPartImages = 2048;   // fewest images per part of a split RIR (one chunk)
 
 struct gpurir_sim {
     int mp = 0, lut = 0;
@@ -354,6 +358,9 @@ struct Plan {
     int tpl, em, nsub, grid, clamp;
     long unfused_tails = 0;   // RIRs whose tail the separate tail kernel writes
     int axis_cap = 0;         // per-axis table entries per block (max over rooms of N0 + N1 + N2)
+    std::vector<PartGroup> groups;   // partial segments to add up (RIRs split by images)
+    long long part_floats = 0;       // size of the partial-segment buffer
+    int max_part_len = 0;
     int mode = 0, tw = 0;   // tap evaluation mode (0 FP32, 1 mixed precision, 2 LUT), window length
     int max_n_diff;
     std::vector<IsmItem> items;
@@ -398,6 +405,9 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     }
     P.items.clear();
     P.rirs.clear();
+    P.groups.clear();
+    P.part_floats = 0;
+    P.max_part_len = 0;
     P.unfused_tails = 0;
     P.rirs.reserve(M_tot);
     const long seg_max = std::min<long>((long)max_nsub * sub, 16384);   // int16 image offsets
@@ -411,17 +421,24 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     for (size_t ri = 0; ri < R.size(); ri++) {
         const RoomDesc &r = R[ri];
         const long M = (long)r.n_src * r.n_rcv;
-        long n_seg = 0, tseg = 0;
+        long n_seg = 0, tseg = 0, n_part = 1;
         if (r.n_ism > 0) {
             const long min_seg = (r.n_ism + seg_max - 1) / seg_max;
             const long cap = (r.n_ism + sub - 1) / sub;
-            n_seg = std::max(min_seg, std::min(want, cap));
+            // Small launches need more items than RIRs.  Splitting an RIR's images into
+            // parts (partial segments added up afterwards) costs no extra image work;
+            // cutting its time axis finer makes every segment walk all the images.  So
+            // parts first, at least kPartImages images each, then finer segments.
+            n_part = std::max<long>(1, std::min<long>((want + min_seg - 1) / min_seg,
+                                                        r.n_img / kPartImages));
+            n_seg = std::max(min_seg, std::min((want + n_part - 1) / n_part, cap));
             tseg = std::min<long>(align_up((size_t)((r.n_ism + n_seg - 1) / n_seg), 32), seg_max);
             n_seg = (r.n_ism + tseg - 1) / tseg;
             P.nsub = std::max<int>(P.nsub, (int)((tseg + sub - 1) / sub));
         }
-        // a single-segment RIR gets its tail from the ISM kernel's epilogue
-        const bool fused = n_seg == 1 && r.n_total > r.n_ism;
+        // a single-segment RIR holding all its images gets its tail from the ISM
+        // kernel's epilogue
+        const bool fused = n_seg == 1 && n_part == 1 && r.n_total > r.n_ism;
         for (long m = 0; m < M; m++) {
             IsmItem it{};
             it.room = (int)ri;
@@ -437,11 +454,25 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
                 IsmItem w = it;
                 w.t_lo = (int)(g * tseg);
                 w.t_hi = (int)std::min<long>((g + 1) * tseg, r.n_ism);
+                w.part_off = -1;
+                const int len = w.t_hi - w.t_lo;
+                if (n_part > 1) {
+                    P.groups.push_back({it.out_row + w.t_lo, P.part_floats, len, (int)n_part});
+                    P.max_part_len = std::max(P.max_part_len, len);
+                }
                 // images in the segment's delay range (density grows with delay^2), plus
-                // the geometry pass over every image of the room
+                // the geometry pass over every image of the part
                 const double a = (double)w.t_lo / r.n_ism, b = (double)w.t_hi / r.n_ism;
-                cost.push_back({r.n_img * ((b * b * b - a * a * a) + 0.15), (int)work.size()});
-                work.push_back(w);
+                for (long p = 0; p < n_part; p++) {
+                    w.i_lo = (int)((long long)r.n_img * p / n_part);
+                    w.i_hi = (int)((long long)r.n_img * (p + 1) / n_part);
+                    if (n_part > 1) {
+                        w.part_off = P.part_floats;
+                        P.part_floats += len;
+                    }
+                    cost.push_back({(w.i_hi - w.i_lo) * ((b * b * b - a * a * a) + 0.15), (int)work.size()});
+                    work.push_back(w);
+                }
             }
         }
     }
@@ -474,7 +505,7 @@ static int check_status(gpurir_sim *s) {
 
 // Byte layout of one launch's descriptors (mirrored host staging -> device).
 struct Layout {
-    size_t o_rooms, o_items, o_rirs, o_pos, stage_bytes, o_env, o_axis, o_out, dev_bytes;
+    size_t o_rooms, o_items, o_rirs, o_groups, o_pos, stage_bytes, o_env, o_axis, o_part, o_out, dev_bytes;
 };
 
 static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv, long M,
@@ -483,12 +514,14 @@ static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv,
     L.o_rooms = 0;
     L.o_items = align_up(L.o_rooms + n_rooms * sizeof(RoomDesc), 256);
     L.o_rirs = align_up(L.o_items + P.items.size() * sizeof(IsmItem), 256);
-    L.o_pos = align_up(L.o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
+    L.o_groups = align_up(L.o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
+    L.o_pos = align_up(L.o_groups + P.groups.size() * sizeof(PartGroup), 256);
     size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
     L.stage_bytes = align_up(L.o_pos + n_pos * sizeof(float), 256);
     L.o_env = L.stage_bytes;
     L.o_axis = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
-    L.o_out = align_up(L.o_axis + (size_t)P.grid * P.axis_cap * sizeof(float4), 256);
+    L.o_part = align_up(L.o_axis + (size_t)P.grid * P.axis_cap * sizeof(float4), 256);
+    L.o_out = align_up(L.o_part + (size_t)P.part_floats * sizeof(float), 256);
     L.dev_bytes = L.o_out + (host_io ? (size_t)out_elems * sizeof(float) : 0);
     return L;
 }
@@ -497,6 +530,7 @@ static void fill_stage(char *h, const Layout &L, const std::vector<RoomDesc> &R,
     memcpy(h + L.o_rooms, R.data(), R.size() * sizeof(RoomDesc));
     if (!P.items.empty()) memcpy(h + L.o_items, P.items.data(), P.items.size() * sizeof(IsmItem));
     if (!P.rirs.empty()) memcpy(h + L.o_rirs, P.rirs.data(), P.rirs.size() * sizeof(IsmItem));
+    if (!P.groups.empty()) memcpy(h + L.o_groups, P.groups.data(), P.groups.size() * sizeof(PartGroup));
 }
 
 // Enqueue the ISM and tail kernels of one planned launch on `st`.
@@ -518,7 +552,13 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
                               s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw, &ta,
-                              reinterpret_cast<float4 *>(const_cast<char *>(d) + L.o_axis), P.axis_cap));
+                              reinterpret_cast<float4 *>(const_cast<char *>(d) + L.o_axis), P.axis_cap,
+                              reinterpret_cast<float *>(const_cast<char *>(d) + L.o_part)));
+    if (!P.groups.empty()) {   // RIRs split by images: add up their partial segments
+        if (record) s->last_launches += 1;
+        CK(partial_reduce_launch(reinterpret_cast<const PartGroup *>(d + L.o_groups), (int)P.groups.size(),
+                                 P.max_part_len, reinterpret_cast<const float *>(d + L.o_part), dout, st));
+    }
     if (record && s->ev_ism) CK(cudaEventRecord(s->ev[1], st));
     const bool tail_kernel = P.max_n_diff > 0 && (P.unfused_tails > 0 || P.grid == 0);
     if (record && s->profile && tail_kernel) { CK(cudaEventRecord(s->ev[2], st)); s->ev_tail = true; }

@@ -40,13 +40,25 @@ struct RoomDesc {
     float pw[6][kPowMax];  // pw[w][k] = (-beta[w])^k, rounded from FP64
 };
 
-// One work item of the persistent ISM kernel: one RIR, one segment of samples.
+// One work item of the persistent ISM kernel: one RIR, one segment of samples, one
+// range of its images.  An item holding all the images writes the segment into the
+// output; an item holding a part of them writes a partial segment (part_off >= 0)
+// that a reduction adds up with the RIR's other parts in a fixed order.
 struct IsmItem {
     int room;       // index into the RoomDesc table
     int src, rcv;   // rows of the position arrays (global)
     int t_lo, t_hi; // output samples [t_lo, t_hi) of the early part
     int rir;        // global RIR index
-    long long out_row;  // element offset of sample 0 of this RIR in the output
+    long long out_row;   // element offset of sample 0 of this RIR in the output
+    int i_lo, i_hi;      // images [i_lo, i_hi) of the room's image grid
+    long long part_off;  // -1, or the offset of this item's partial segment
+};
+
+// A set of partial segments to add up: out[out + t] = sum_p part[base + p len + t].
+struct PartGroup {
+    long long out;    // element offset of the segment's first sample in the output
+    long long base;   // offset of the first partial segment
+    int len, n_part;
 };
 
 // ---------------------------------------------------------------------------

@@ -136,7 +136,8 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
 #pragma unroll
         for (int q = 0; q < kGrad; q++) acc[q] = 0.0f;
 
-        for (int cbase = 0; cbase < n_img; cbase += kBChunk) {
+        const int i_end = min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
+        for (int cbase = it.i_lo; cbase < i_end; cbase += kBChunk) {
             // ---- pass A: geometry, keep images whose window meets the segment (image order)
             int kept_mine = 0;
             int keep_flag[kBRounds];
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                 rg[r] = 1.f;
                 rn0[r] = 0;
                 ridx[r] = i;
-                if (i < n_img) {
+                if (i < i_end) {
                     int q, m2, m0, m1;
                     divmod_small(i, N2, rN2, q, m2);
                     divmod_small(q, N1, rN1, m0, m1);

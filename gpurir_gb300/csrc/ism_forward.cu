@@ -68,6 +68,7 @@ struct IsmLaunch {
     // N1, then N2 entries.  nullptr: computed per image instead.
     float4 *axis_tab;
     int axis_cap;
+    float *partial;   // partial segments of items holding a part of an RIR's images
 };
 
 // Evaluation modes of the taps (template parameter MODE):
@@ -314,9 +315,10 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         // reach, nothing can be skipped and the test is not made
         const float x_max = (float)(N0 / 2 + 1) * L0, y_max = (float)(N1 / 2 + 1) * L1;
         const bool may_skip = use_tab && x_max * x_max + y_max * y_max > dhi2;
-        for (int cbase = 0; cbase < n_img; cbase += kChunk) {
+        const int i_end = min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
+        for (int cbase = it.i_lo; cbase < i_end; cbase += kChunk) {
             if (may_skip) {
-                const int q_first = cbase / N2, q_last = (min(cbase + kChunk, n_img) - 1) / N2;
+                const int q_first = cbase / N2, q_last = (min(cbase + kChunk, i_end) - 1) / N2;
                 int hit = 0;
                 for (int q = q_first + tid; q <= q_last && !hit; q += kThreads) {
                     int m0, m1;
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 int sub = -1;
                 float a = 0.f, f = 0.f, sphi = 0.f, cphi = 1.f;
                 int n0 = 0;
-                if (i < n_img) {
+                if (i < i_end) {
                     int q, m2, m0, m1;
                     divmod_small(i, N2, rN2, q, m2);
                     divmod_small(q, N1, rN1, m0, m1);
@@ -559,8 +561,10 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         // ---- output: sum of the covering sub-range buffers, ascending s.  An item that
         //      holds a whole early part also predicts the envelope from it and writes the
         //      diffuse tail, so those stores overlap other blocks' tap work.
-        float *orow = P.out + it.out_row;
-        const bool fuse = P.fuse_tail && t_lo == 0 && t_hi == R.n_ism && R.n_total > R.n_ism;
+        // a partial item writes its segment at part_off (sample t_lo first)
+        float *orow = it.part_off >= 0 ? P.partial + it.part_off - t_lo : P.out + it.out_row;
+        const bool fuse = P.fuse_tail && it.part_off < 0 && t_lo == 0 && t_hi == R.n_ism &&
+                          R.n_total > R.n_ism;
         float tau_dp = 0.0f;
         int w_start = t_hi;
         if (fuse) {
@@ -719,10 +723,12 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap) {
+                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
+                               float *partial) {
     IsmLaunch p;
     p.axis_tab = axis_tab;
     p.axis_cap = axis_cap;
+    p.partial = partial;
     p.seed = tail ? tail->seed : 0;
     p.offset = tail ? tail->offset : 0;
     p.offset_ptr = tail ? tail->offset_ptr : nullptr;
@@ -742,6 +748,29 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
     case kModeLUT: return launch_mode<kModeLUT>(tpl, p, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
+}
+
+// Sum of the partial segments of each group, parts in increasing order (the result
+// does not depend on which block computed which part).
+__global__ void partial_reduce_kernel(const PartGroup *groups, int n_groups, const float *part, float *out) {
+    const int g = blockIdx.y;
+    if (g >= n_groups) return;
+    const PartGroup G = groups[g];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.len) return;
+    const float *p = part + G.base + t;
+    float acc = 0.0f;
+    for (int k = 0; k < G.n_part; k++) acc += p[(long long)k * G.len];
+    out[G.out + t] = acc;
+}
+
+cudaError_t partial_reduce_launch(const PartGroup *groups, int n_groups, int max_len, const float *part,
+                                  float *out, cudaStream_t st) {
+    if (n_groups <= 0 || max_len <= 0) return cudaSuccess;
+    if (n_groups > 65535) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((max_len + 255) / 256), (unsigned)n_groups);
+    partial_reduce_kernel<<<grid, 256, 0, st>>>(groups, n_groups, part, out);
+    return cudaGetLastError();
 }
 
 }  // namespace gpurir

@@ -24,7 +24,8 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *pos_src, const float *pos_rcv, const float *orv_src,
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
-                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap);
+                               int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
+                               float *partial);
 int describe_room(RoomDesc &R, const float room[3], const float beta[6], const int nb[3], float Tdiff,
                   float Tmax, float Fs, float c, int spkr, int mic);
 int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub);
@@ -40,7 +41,7 @@ constexpr size_t kNoAllocRoom = (sizeof(RoomDesc) + 255) / 256 * 256;
 constexpr size_t kNoAllocBytes = kNoAllocCtl + kNoAllocRoom + (size_t)kNoAllocMaxItems * sizeof(IsmItem);
 
 // The scratch: 256 B of control words, one RoomDesc, kNoAllocMaxItems IsmItems
-// (about 260 KB).  Shared by every call on this device.
+// (about 390 KB).  Shared by every call on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Device address of the scratch, looked up once per device with that device current.
@@ -88,6 +89,9 @@ __global__ void noalloc_prepare_kernel(RoomDesc R, long M, int M_rcv, long n_seg
     it.out_row = (long long)m * R.n_ism;
     it.t_lo = (int)(g * tseg);
     it.t_hi = (int)min((g + 1) * tseg, (long)R.n_ism);
+    it.i_lo = 0;
+    it.i_hi = R.n_img;
+    it.part_off = -1;
     items[k] = it;
 }
 
@@ -154,7 +158,7 @@ extern "C" int gpurir_simulate_ism_noalloc(const float room_sz[3], const float b
     if (cudaGetLastError() != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: prepare launch failed");
     if (ism_forward_launch(tpl, d_room, d_items, (int)n_items, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
-                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st, 0, tw, nullptr, nullptr, 0) != cudaSuccess)
+                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st, 0, tw, nullptr, nullptr, 0, nullptr) != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: kernel launch failed");
     return GPURIR_OK;
 }

@@ -223,7 +223,7 @@ int gpurir_trajectory(gpurir_sim *sim, const float *segments, int n_pts, int seg
  * in the reference.  For callers that must not call cudaMalloc while they run:
  * real-time audio threads (cudaMalloc may block on a device synchronisation),
  * hosts with a fixed device-memory budget, work recorded under global stream
- * capture.  The kernel's scratch is a fixed ~260 KB array in this library,
+ * capture.  The kernel's scratch is a fixed ~390 KB array in this library,
  * held on every GPU that loads it until the process exits; calls are limited to
  * 8192 RIRs x segments (M_src * M_rcv <= 8192) and fail with GPURIR_ERR_INVALID
  * beyond.  Computes the image-source part only, as gpurir_simulate_rir_device
