@@ -233,3 +233,14 @@ def test_training_step_in_a_cuda_graph(built):
     torch.cuda.synchronize()
     assert torch.equal(beta.grad, eager[0]) and torch.equal(ps.grad, eager[1])
     assert model.status() == 0
+
+
+def test_gradients_with_rirs_split_by_images(built):
+    """A small launch with many images (1 x 2 RIRs, 17^3 images): the planner splits
+    each RIR's images into parts; forward and adjoint still match FP64 autograd."""
+    c = _setup(41, "card", "omni", ns=1, nr=2, nb=(17, 17, 17), T=0.05)
+    ours, h = _ours(c)
+    ref, href = _ref(c)
+    assert rel_l2(h.detach().cpu().numpy(), href) < 1e-5
+    for k in ours:
+        assert rel_l2(ours[k], ref[k]) < TOL, k

@@ -251,3 +251,17 @@ def test_too_many_images_is_an_error(built):
     with pytest.raises(G.GpuRirError):
         _sim().simulate_rir([3, 3, 3], [0.5] * 6, ps, ps + 0.5, None, None, 0, 0, [300, 300, 300],
                             0.01, 0.01, 16000.0)
+
+
+def test_rirs_split_by_images_with_tail(built):
+    """Few RIRs with many images: each RIR's images are split into parts whose partial
+    early parts a reduction adds up; the tail kernel then reads the finished early part."""
+    rng = np.random.default_rng(17)
+    room = [5.0, 4.0, 3.0]
+    ps = _rand_inside(rng, 1, room, 0.5)
+    pr = _rand_inside(rng, 2, room, 0.5)
+    out, ref, p = _run(_sim(), room, [0.85] * 6, ps, pr, [21, 21, 21], 0.3, 16000.0, Tdiff=0.08)
+    _check_ism(out, ref, p["n_ism"], "split")
+    n = p["n_ism"]
+    assert np.all(p["A"] > 0)
+    assert rel_l2(out[..., n:], ref[..., n:]) <= 1e-4
