@@ -28,7 +28,9 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
                                int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
-                               float *partial);
+                               float *partial, const unsigned char *skip);
+cudaError_t item_skip_launch(const RoomDesc *rooms, const IsmItem *items, int n_items, const float *pos_src,
+                             const float *pos_rcv, unsigned char *skip, cudaStream_t st);
 cudaError_t partial_reduce_launch(const PartGroup *groups, int n_groups, int max_len, const float *part,
                                   float *out, cudaStream_t st);
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
@@ -44,8 +46,9 @@ cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *i
                                 const float *orv_rcv, const float *grad, float *item_grad,
                                 int *work_counter, int *status, int max_tseg, int grid, int clamp,
                                 cudaStream_t st);
-cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
-                               int comp_lo, int n_comp, float *out, cudaStream_t st);
+cudaError_t grad_reduce_launch(const float *item_grad, const int *const csr[6], int n_rooms, int n_src,
+                               int n_rcv, float *const out[5], cudaStream_t st);
+int ism_backward_blocks_per_sm(int tpl, int clamp, size_t smem);
 size_t fft_smem_bytes(int M);
 size_t fft_scratch_floats2(int M, int grid);
 cudaError_t twiddle_launch(float2 *w, int n, cudaStream_t st);
@@ -363,6 +366,7 @@ struct Plan {
     int max_part_len = 0;
     int mode = 0, tw = 0;   // tap evaluation mode (0 FP32, 1 mixed precision, 2 LUT), window length
     int max_n_diff;
+    bool skip_flags = false;   // some segment starts past the rooms' delay bound: test items on the device
     std::vector<IsmItem> items;
     std::vector<IsmItem> rirs;
 };
@@ -405,6 +409,7 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     }
     P.items.clear();
     P.rirs.clear();
+    P.skip_flags = false;
     P.groups.clear();
     P.part_floats = 0;
     P.max_part_len = 0;
@@ -421,7 +426,22 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     for (size_t ri = 0; ri < R.size(); ri++) {
         const RoomDesc &r = R[ri];
         const long M = (long)r.n_src * r.n_rcv;
-        long n_seg = 0, tseg = 0, n_part = 1;
+        long n_seg = 0, n_part = 1;
+        std::vector<std::pair<int, int>> segs;   // [t_lo, t_hi) of each segment
+        // Latest delay of any image while source and receiver are inside the room:
+        // |receiver -> image| <= (N/2 + 1) L per axis.  Only an estimate for the cost
+        // order (segments beyond it hold no image); the kernels test each item against
+        // the actual positions and skip the image work of segments no image reaches.
+        double reach2 = 0.0;
+        for (int a = 0; a < 3; a++) {
+            const double e = (double)(r.nb[a] / 2 + 1) * r.L[a];
+            reach2 += e * e;
+        }
+        const double span = std::sqrt(reach2) * ((double)r.kh + r.kl) + r.H + 2.0;
+        auto cut = [&](long lo, long hi, long n) {   // n segments of [lo, hi), 32-aligned
+            const long t = std::min<long>(align_up((size_t)((hi - lo + n - 1) / n), 32), seg_max);
+            for (long a = lo; a < hi; a += t) segs.push_back({(int)a, (int)std::min(a + t, hi)});
+        };
         if (r.n_ism > 0) {
             const long min_seg = (r.n_ism + seg_max - 1) / seg_max;
             const long cap = (r.n_ism + sub - 1) / sub;
@@ -432,9 +452,12 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
             n_part = std::max<long>(1, std::min<long>((want + min_seg - 1) / min_seg,
                                                         r.n_img / kPartImages));
             n_seg = std::max(min_seg, std::min((want + n_part - 1) / n_part, cap));
-            tseg = std::min<long>(align_up((size_t)((r.n_ism + n_seg - 1) / n_seg), 32), seg_max);
-            n_seg = (r.n_ism + tseg - 1) / tseg;
-            P.nsub = std::max<int>(P.nsub, (int)((tseg + sub - 1) / sub));
+            // (cutting only the images' span finer, and the zeros after it into few long
+            // segments, was slower on small launches: more items, each with its fixed
+            // setup, planning and output)
+            cut(0, r.n_ism, n_seg);
+            n_seg = (long)segs.size();
+            for (auto &g : segs) P.nsub = std::max<int>(P.nsub, (g.second - g.first + sub - 1) / sub);
         }
         // a single-segment RIR holding all its images gets its tail from the ISM
         // kernel's epilogue
@@ -452,17 +475,20 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
             if (!fused && r.n_total > r.n_ism) P.unfused_tails++;
             for (long g = 0; g < n_seg; g++) {
                 IsmItem w = it;
-                w.t_lo = (int)(g * tseg);
-                w.t_hi = (int)std::min<long>((g + 1) * tseg, r.n_ism);
+                w.t_lo = segs[g].first;
+                w.t_hi = segs[g].second;
                 w.part_off = -1;
                 const int len = w.t_hi - w.t_lo;
                 if (n_part > 1) {
                     P.groups.push_back({it.out_row + w.t_lo, P.part_floats, len, (int)n_part});
                     P.max_part_len = std::max(P.max_part_len, len);
                 }
-                // images in the segment's delay range (density grows with delay^2), plus
-                // the geometry pass over every image of the part
-                const double a = (double)w.t_lo / r.n_ism, b = (double)w.t_hi / r.n_ism;
+                // images in the segment's delay range (density grows with delay^2, none
+                // beyond the span), the geometry pass over every image of the part when
+                // any can reach the segment, and the samples written
+                const double S = std::max(span, 1.0);
+                const double a = std::min<double>(w.t_lo, S) / S, b = std::min<double>(w.t_hi, S) / S;
+                const double walk = w.t_lo < S ? 0.15 : 0.0;
                 for (long p = 0; p < n_part; p++) {
                     w.i_lo = (int)((long long)r.n_img * p / n_part);
                     w.i_hi = (int)((long long)r.n_img * (p + 1) / n_part);
@@ -470,7 +496,9 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
                         w.part_off = P.part_floats;
                         P.part_floats += len;
                     }
-                    cost.push_back({(w.i_hi - w.i_lo) * ((b * b * b - a * a * a) + 0.15), (int)work.size()});
+                    cost.push_back({(w.i_hi - w.i_lo) * ((b * b * b - a * a * a) + walk) + 2e-3 * len,
+                                    (int)work.size()});
+                    P.skip_flags |= w.t_lo > 0 && w.t_lo >= S;
                     work.push_back(w);
                 }
             }
@@ -485,6 +513,7 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
                                                       const std::pair<double, int> &y) { return x.first > y.first; });
     P.items.reserve(work.size());
     for (auto &c : cost) P.items.push_back(work[c.second]);
+
     P.grid = 0;
     if (P.items.empty()) return GPURIR_OK;
     size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub, P.mode, P.tw);
@@ -505,7 +534,8 @@ static int check_status(gpurir_sim *s) {
 
 // Byte layout of one launch's descriptors (mirrored host staging -> device).
 struct Layout {
-    size_t o_rooms, o_items, o_rirs, o_groups, o_pos, stage_bytes, o_env, o_axis, o_part, o_out, dev_bytes;
+    size_t o_rooms, o_items, o_rirs, o_groups, o_pos, stage_bytes, o_env, o_axis, o_part, o_skip, o_out,
+        dev_bytes;
 };
 
 static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv, long M,
@@ -521,7 +551,8 @@ static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv,
     L.o_env = L.stage_bytes;
     L.o_axis = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
     L.o_part = align_up(L.o_axis + (size_t)P.grid * P.axis_cap * sizeof(float4), 256);
-    L.o_out = align_up(L.o_part + (size_t)P.part_floats * sizeof(float), 256);
+    L.o_skip = align_up(L.o_part + (size_t)P.part_floats * sizeof(float), 256);
+    L.o_out = align_up(L.o_skip + (P.skip_flags ? P.items.size() : 0), 256);
     L.dev_bytes = L.o_out + (host_io ? (size_t)out_elems * sizeof(float) : 0);
     return L;
 }
@@ -548,12 +579,19 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     ta.env_out = reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env);
     ta.fuse = 1;
     if (record) s->last_launches = (P.grid > 0 ? 1 : 0);
+    unsigned char *skip = nullptr;
+    if (P.grid > 0 && P.skip_flags) {   // segments no image may reach: flags at the current positions
+        skip = reinterpret_cast<unsigned char *>(const_cast<char *>(d) + L.o_skip);
+        CK(item_skip_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_items), (int)P.items.size(),
+                            dps, dpr, skip, st));
+        if (record) s->last_launches += 1;
+    }
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
                               (int)P.items.size(), dps, dpr, dos, dor, dout, work_counter,
                               s->d_ctl + 1, P.em, P.nsub, P.clamp, P.grid, st, P.mode, P.tw, &ta,
                               reinterpret_cast<float4 *>(const_cast<char *>(d) + L.o_axis), P.axis_cap,
-                              reinterpret_cast<float *>(const_cast<char *>(d) + L.o_part)));
+                              reinterpret_cast<float *>(const_cast<char *>(d) + L.o_part), skip));
     if (!P.groups.empty()) {   // RIRs split by images: add up their partial segments
         if (record) s->last_launches += 1;
         CK(partial_reduce_launch(reinterpret_cast<const PartGroup *>(d + L.o_groups), (int)P.groups.size(),
@@ -1061,7 +1099,9 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
         const int pad = 64 * P.tpl;
         const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad);
         if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
-        const int grid = std::min(n_items, s->num_sms);   // one 512-thread block per SM (registers)
+        const int bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, smem);
+        if (bps < 1) return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
+        const int grid = std::min(n_items, s->num_sms * bps);
         CK(ism_backward_launch(P.tpl, reinterpret_cast<const RoomDesc *>(d + o_rooms),
                                reinterpret_cast<const IsmItem *>(d + o_items), n_items, d_pos_src,
                                d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, s->d_ctl, s->d_ctl + 1,
@@ -1069,11 +1109,8 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     }
     const int *dp[6];
     for (int a = 0; a < 6; a++) dp[a] = reinterpret_cast<const int *>(d + o_arr[a]);
-    if (d_grad_beta) CK(grad_reduce_launch(ig, dp[0], dp[1], n_rooms, 0, 6, d_grad_beta, st));
-    if (d_grad_pos_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)ns, 6, 3, d_grad_pos_src, st));
-    if (d_grad_pos_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)nr, 9, 3, d_grad_pos_rcv, st));
-    if (d_grad_orV_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)ns, 12, 3, d_grad_orV_src, st));
-    if (d_grad_orV_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)nr, 15, 3, d_grad_orV_rcv, st));
+    float *const outs[5] = {d_grad_beta, d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src, d_grad_orV_rcv};
+    CK(grad_reduce_launch(ig, dp, n_rooms, (int)ns, (int)nr, outs, st));
     CK(cudaEventRecord(s->ws_busy, st));
     s->ws_recorded = true;
     return GPURIR_OK;
@@ -1128,7 +1165,14 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
         delete a;
         return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
     }
-    a->grid_b = std::min(n_items, s->num_sms);
+    if (n_items > 0) {
+        const int bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl));
+        if (bps < 1) {
+            delete a;
+            return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
+        }
+        a->grid_b = std::min(n_items, s->num_sms * bps);
+    }
     std::vector<int> lists[6];
     csr(P.items, n_rooms, &IsmItem::room, 0, lists[0], lists[1]);
     csr(P.items, (int)a->ns, &IsmItem::src, 0, lists[2], lists[3]);
@@ -1195,11 +1239,8 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
     }
     const int *dp[6];
     for (int k = 0; k < 6; k++) dp[k] = reinterpret_cast<const int *>(a->d + a->o_arr[k]);
-    if (d_grad_beta) CK(grad_reduce_launch(ig, dp[0], dp[1], a->n_rooms, 0, 6, d_grad_beta, st));
-    if (d_grad_pos_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)a->ns, 6, 3, d_grad_pos_src, st));
-    if (d_grad_pos_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)a->nr, 9, 3, d_grad_pos_rcv, st));
-    if (d_grad_orV_src) CK(grad_reduce_launch(ig, dp[2], dp[3], (int)a->ns, 12, 3, d_grad_orV_src, st));
-    if (d_grad_orV_rcv) CK(grad_reduce_launch(ig, dp[4], dp[5], (int)a->nr, 15, 3, d_grad_orV_rcv, st));
+    float *const outs[5] = {d_grad_beta, d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src, d_grad_orV_rcv};
+    CK(grad_reduce_launch(ig, dp, a->n_rooms, (int)a->ns, (int)a->nr, outs, st));
     return GPURIR_OK;
 }
 

@@ -199,6 +199,46 @@ __device__ __forceinline__ void image_axis(int n, int N, int &clust, int &refl) 
     refl = k & 1;           // |k % 2| in two's complement
 }
 
+// Range of the squared receiver->image component along one axis over all N images
+// of that axis, for any source and receiver coordinates.  The image coordinate is
+// k L + s for even k and (k + 1) L - s for odd k: each parity is increasing in k, so
+// its extremes are at its first and last index and it crosses zero at most once.
+// Plain FP32 (a bound to a few 1e-6 relative; callers leave a margin).
+__device__ __forceinline__ void axis_extent(int N, float L, float s, float r, float &v2min, float &v2max) {
+    const int k_min = -(N / 2), k_max = N - 1 - N / 2;
+    v2min = 3.0e38f;
+    v2max = 0.0f;
+#pragma unroll
+    for (int par = 0; par < 2; par++) {
+        const int lo = (k_min & 1) == par ? k_min : k_min + 1;
+        const int hi = (k_max & 1) == par ? k_max : k_max - 1;
+        if (lo > hi) continue;
+        const float a = par ? (float)(lo + 1) * L - s - r : (float)lo * L + s - r;
+        const float b = par ? (float)(hi + 1) * L - s - r : (float)hi * L + s - r;
+        v2max = fmaxf(v2max, fmaxf(a * a, b * b));
+        v2min = fminf(v2min, (a <= 0.0f && b >= 0.0f) ? 0.0f : fminf(a * a, b * b));
+    }
+}
+
+// True when no image of the pair (src, rcv) has a delay within reach of the samples
+// [t_lo, t_hi): every delay lies below t_lo - H - margin or above t_hi + H + margin.
+// fs_c = Fs / c in samples per metre.
+__device__ __forceinline__ bool images_miss_segment(const float L[3], const int nb[3], const float s[3],
+                                                    const float r[3], float fs_c, float H, int t_lo,
+                                                    int t_hi) {
+    float lo2 = 0.0f, hi2 = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float mn, mx;
+        axis_extent(nb[a], L[a], s[a], r[a], mn, mx);
+        lo2 += mn;
+        hi2 += mx;
+    }
+    const float tau_lo = sqrtf(lo2) * fs_c, tau_hi = sqrtf(hi2) * fs_c;
+    const float margin = 2.0f + 1e-5f * tau_hi;
+    return tau_hi < (float)t_lo - H - margin || tau_lo > (float)t_hi + H + margin;
+}
+
 // Directivity gain, src/gpuRIR_cuda.cu:132-147, with the cosine already formed.
 __device__ __forceinline__ float pattern_gain(float cos_t, int pattern) {
     switch (pattern) {

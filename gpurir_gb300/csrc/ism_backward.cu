@@ -22,9 +22,9 @@
 
 namespace gpurir {
 
-constexpr int kBThreads = 512;
+constexpr int kBThreads = 256;   // two blocks per SM (registers): one block's barriers overlap the other's work
 constexpr int kBWarps = kBThreads / 32;
-constexpr int kBChunk = 1024;
+constexpr int kBChunk = 512;
 constexpr int kBRounds = kBChunk / kBThreads;   // images per lane and chunk
 constexpr int kGrad = 18;                       // beta[6], src[3], rcv[3], orv_src[3], orv_rcv[3]
 
@@ -60,7 +60,7 @@ __device__ __forceinline__ float pattern_slope(int pattern) {
 }
 
 template <int TPL, bool CLAMP>
-__global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P) {
+__global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P) {
     constexpr int KS = 32 * TPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4 *rec = reinterpret_cast<float4 *>(smem_raw);          // sigma, f, cos phi, sin phi
@@ -89,13 +89,6 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
             __syncthreads();
             continue;
         }
-        // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment.
-        const int g_len = t_hi - t_lo + 2 * P.pad;
-        const float *grow = P.grad + it.out_row;
-        for (int i = tid; i < g_len; i += kBThreads) {
-            const int t = t_lo - P.pad + i;
-            gs[i] = (t >= t_lo && t < t_hi) ? grow[t] : 0.0f;
-        }
         const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
         const int N0 = R.nb[0], N1 = R.nb[1], N2 = R.nb[2];
         const int n_img = R.n_img;
@@ -118,6 +111,22 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
         }
         const float keep_lo = (float)t_lo - H, keep_hi = (float)t_hi + H;
         const float fs_c = R.kh + R.kl;   // Fs / c
+        // an item whose segment no image reaches contributes nothing: no staging, no chunks
+        // (tested on later segments; a first segment holds the direct path)
+        bool miss = false;
+        if (t_lo > 0) {
+            const float Lr[3] = {L0, L1, L2}, s3[3] = {sx, sy, sz}, r3[3] = {rx, ry, rz};
+            miss = images_miss_segment(Lr, R.nb, s3, r3, R.kh, H, t_lo, t_hi);
+        }
+        // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment.
+        if (!miss) {
+            const int g_len = t_hi - t_lo + 2 * P.pad;
+            const float *grow = P.grad + it.out_row;
+            for (int i = tid; i < g_len; i += kBThreads) {
+                const int t = t_lo - P.pad + i;
+                gs[i] = (t >= t_lo && t < t_hi) ? grow[t] : 0.0f;
+            }
+        }
         const float dws = 3.14159265358979323846f * inv_h;   // 2 pi / Tw
         // per-lane tap constants
         float kf[TPL], ck[TPL], sk[TPL], ckd[TPL], skd[TPL];   // ckd, skd: times 2 pi / Tw
@@ -136,7 +145,7 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
 #pragma unroll
         for (int q = 0; q < kGrad; q++) acc[q] = 0.0f;
 
-        const int i_end = min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
+        const int i_end = miss ? it.i_lo : min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
         for (int cbase = it.i_lo; cbase < i_end; cbase += kBChunk) {
             // ---- pass A: geometry, keep images whose window meets the segment (image order)
             int kept_mine = 0;
@@ -240,19 +249,23 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
                         const float sig = c.x * lane_sign, f = c.y, cphi = c.z, sphi = c.w;
                         const float gam = rec_gamma[jj] * lane_sign;
                         const float *gp = gl + rec_n0[jj] + k_lo;
+                        // sigma and gamma are constant over the image: with q = g / x,
+                        //   sum g W  = sigma S,   S = sum q w
+                        //   sum g W' = sigma T + gamma S,   T = sum q (w' - w / x)
+                        float s1 = 0.0f, t1 = 0.0f;
 #pragma unroll
                         for (int i = 0; i < TPL; i++) {
                             const float x = kf[i] - f;
                             const float rx_ = rcp_approx_b(x);
                             const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
                             const float wd = fmaf(ckd[i], sphi, -skd[i] * cphi);
-                            const float s = sig * rx_;
-                            float W = w * s, Wd = fmaf(wd, s, w * ((gam - s) * rx_));
-                            if (CLAMP && fabsf(x) >= H) { W = 0.0f; Wd = 0.0f; }
-                            const float g = gp[32 * i];
-                            a[u] = fmaf(g, W, a[u]);
-                            b[u] = fmaf(g, Wd, b[u]);
+                            float q = gp[32 * i] * rx_;
+                            if (CLAMP && fabsf(x) >= H) q = 0.0f;
+                            s1 = fmaf(q, w, s1);
+                            t1 = fmaf(q, fmaf(-w, rx_, wd), t1);
                         }
+                        a[u] = sig * s1;
+                        b[u] = fmaf(sig, t1, gam * s1);
                     }
                     if (j + 1 >= j1) { a[1] = 0.f; b[1] = 0.f; }
                     // reduce 4 values over the warp with 6 shuffles
@@ -380,17 +393,40 @@ __global__ void __launch_bounds__(kBThreads, 1) ism_backward_kernel(BwdLaunch P)
     }
 }
 
-// Sum of item partials per target, in the order of the CSR lists (deterministic).
-//   target t: components [comp_lo, comp_lo + n_comp) of the items list[ptr[t]..ptr[t+1])
-//   are summed into out[t * n_comp + c].
-__global__ void grad_reduce_kernel(const float *item_grad, const int *ptr, const int *list, int n_target,
-                                   int comp_lo, int n_comp, float *out) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_target * n_comp) return;
-    const int t = e / n_comp, c = e - t * n_comp;
-    float s = 0.0f;
-    for (int p = ptr[t]; p < ptr[t + 1]; p++) s += item_grad[(long)list[p] * kGrad + comp_lo + c];
-    out[e] = s;
+// Sum of item partials per target: one warp per target of the five sets (rooms:
+// beta; sources: position, orientation; receivers: position, orientation).  Target t
+// of a set sums components [comp_lo, comp_lo + n_comp) of the items list[ptr[t]..
+// ptr[t+1]) into out[t * n_comp + c]: lane l takes list entries l, l + 32, ... in
+// order, then the lanes are added by a fixed xor tree, so the result does not depend
+// on timing.  A set with out == nullptr has no targets.
+struct GradSet {
+    const int *ptr, *list;
+    int n_target, comp_lo, n_comp;
+    float *out;
+};
+struct GradSets {
+    GradSet s[5];
+};
+
+__global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int t = gw, k = 0;
+    while (k < 5 && t >= G.s[k].n_target) t -= G.s[k++].n_target;
+    if (k == 5) return;
+    const GradSet S = G.s[k];
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int p = S.ptr[t] + lane; p < S.ptr[t + 1]; p += 32) {
+        const float *row = item_grad + (long)S.list[p] * kGrad + S.comp_lo;
+#pragma unroll
+        for (int c = 0; c < 6; c++)
+            if (c < S.n_comp) v[c] += row[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+        if (lane == 0 && c < S.n_comp) S.out[t * S.n_comp + c] = v[c];
+    }
 }
 
 size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
@@ -444,13 +480,37 @@ cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *i
     }
 }
 
-cudaError_t grad_reduce_launch(const float *item_grad, const int *ptr, const int *list, int n_target,
-                               int comp_lo, int n_comp, float *out, cudaStream_t st) {
-    const int n = n_target * n_comp;
-    if (n <= 0) return cudaSuccess;
-    grad_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(item_grad, ptr, list, n_target, comp_lo,
-                                                         n_comp, out);
+// One launch for every requested gradient.  csr[0..5] = room ptr/list, source
+// ptr/list, receiver ptr/list; out[0..4] = beta, source position, receiver position,
+// source orientation, receiver orientation (nullptr: not requested).
+cudaError_t grad_reduce_launch(const float *item_grad, const int *const csr[6], int n_rooms, int n_src,
+                               int n_rcv, float *const out[5], cudaStream_t st) {
+    GradSets G;
+    const int n_t[5] = {n_rooms, n_src, n_rcv, n_src, n_rcv};
+    const int which[5] = {0, 1, 2, 1, 2}, lo[5] = {0, 6, 9, 12, 15}, nc[5] = {6, 3, 3, 3, 3};
+    long warps = 0;
+    for (int k = 0; k < 5; k++) {
+        G.s[k] = GradSet{csr[2 * which[k]], csr[2 * which[k] + 1], out[k] ? n_t[k] : 0, lo[k], nc[k], out[k]};
+        warps += G.s[k].n_target;
+    }
+    if (warps <= 0) return cudaSuccess;
+    grad_reduce_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(item_grad, G);
     return cudaGetLastError();
+}
+
+// Resident blocks per SM of the adjoint kernel with `smem` bytes of shared memory.
+int ism_backward_blocks_per_sm(int tpl, int clamp, size_t smem) {
+    int n = 0;
+    switch (tpl * 2 + (clamp ? 1 : 0)) {
+#define OCC(T, C) case 2 * T + C: cudaFuncSetAttribute(ism_backward_kernel<T, (bool)C>, \
+        cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ism_backward_kernel<T, (bool)C>, kBThreads, smem); break;
+        OCC(2, 0) OCC(2, 1) OCC(4, 0) OCC(4, 1) OCC(8, 0) OCC(8, 1)
+        OCC(12, 0) OCC(12, 1) OCC(16, 0) OCC(16, 1) OCC(24, 0) OCC(24, 1)
+#undef OCC
+    default: return 0;
+    }
+    return n;
 }
 
 }  // namespace gpurir

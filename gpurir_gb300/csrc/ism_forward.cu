@@ -69,6 +69,7 @@ struct IsmLaunch {
     float4 *axis_tab;
     int axis_cap;
     float *partial;   // partial segments of items holding a part of an RIR's images
+    const unsigned char *skip;   // per item: 1 = no image reaches its segment (nullptr: none)
 };
 
 // Evaluation modes of the taps (template parameter MODE):
@@ -252,8 +253,12 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const bool small_phi = inv_h <= 0.0625f;   // window angle f / H <= 1/16: polynomials
         // per-axis terms once per item: an image's squared distance is then two
         // float-float additions (the same operations, in the same order, as per image)
+        // an item whose segment no image of its pair reaches (the zeros after the last
+        // image of a long RIR) only writes zeros: no axis table, no chunks (flags from
+        // item_skip_kernel, launched before this kernel when the plan has later segments)
+        const bool miss = P.skip != nullptr && P.skip[item_id] != 0;
         float4 *tab = P.axis_tab ? P.axis_tab + (size_t)blockIdx.x * P.axis_cap : nullptr;
-        const bool use_tab = tab && N0 + N1 + N2 <= P.axis_cap;
+        const bool use_tab = tab && N0 + N1 + N2 <= P.axis_cap && !miss;
         if (use_tab) {
             for (int e = tid; e < N0 + N1 + N2; e += kThreads) {
                 const int a = e < N0 ? 0 : (e < N0 + N1 ? 1 : 2);
@@ -315,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         // reach, nothing can be skipped and the test is not made
         const float x_max = (float)(N0 / 2 + 1) * L0, y_max = (float)(N1 / 2 + 1) * L1;
         const bool may_skip = use_tab && x_max * x_max + y_max * y_max > dhi2;
-        const int i_end = min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
+        const int i_end = miss ? it.i_lo : min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
         for (int cbase = it.i_lo; cbase < i_end; cbase += kChunk) {
             if (may_skip) {
                 const int q_first = cbase / N2, q_last = (min(cbase + kChunk, i_end) - 1) / N2;
@@ -547,13 +552,26 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             }
             __syncthreads();
             // ---- merge the extra slices into their sub-range, in slice order (deterministic)
+            //      (slots of one sub-range are consecutive: a register sum per run of slots,
+            //      added in the same order as one slot at a time)
             {
                 const int n_extra = ctl[3];
-                for (int w = tid; w < BUF; w += kThreads)
-                    for (int slot = 0; slot < n_extra; slot++) {
-                        float *src = pool + slot * slot_words + P.em + w;
-                        buf[P.em + slot_sub[slot] * BUF + w] += *src;
-                        *src = 0.0f;
+                if (n_extra > 0)
+                    for (int w = tid; w < BUF; w += kThreads) {
+                        int cur = slot_sub[0];
+                        float acc = buf[P.em + cur * BUF + w];
+                        for (int slot = 0; slot < n_extra; slot++) {
+                            const int s = slot_sub[slot];
+                            if (s != cur) {
+                                buf[P.em + cur * BUF + w] = acc;
+                                cur = s;
+                                acc = buf[P.em + cur * BUF + w];
+                            }
+                            float *src = pool + slot * slot_words + P.em + w;
+                            acc += *src;
+                            *src = 0.0f;
+                        }
+                        buf[P.em + cur * BUF + w] = acc;
                     }
             }
             __syncthreads();
@@ -724,8 +742,9 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
                                int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
-                               float *partial) {
+                               float *partial, const unsigned char *skip) {
     IsmLaunch p;
+    p.skip = skip;
     p.axis_tab = axis_tab;
     p.axis_cap = axis_cap;
     p.partial = partial;
@@ -748,6 +767,31 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
     case kModeLUT: return launch_mode<kModeLUT>(tpl, p, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
+}
+
+// Per item: 1 when no image of its (source, receiver) pair can reach its segment,
+// from the per-axis extremes of the image coordinates at the current positions.
+// First segments are not tested (they hold the direct path).
+__global__ void item_skip_kernel(const RoomDesc *rooms, const IsmItem *items, int n_items, const float *pos_src,
+                                 const float *pos_rcv, unsigned char *skip) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    const IsmItem it = items[k];
+    unsigned char m = 0;
+    if (it.t_lo > 0) {
+        const RoomDesc &R = rooms[it.room];
+        const float s3[3] = {pos_src[3 * it.src], pos_src[3 * it.src + 1], pos_src[3 * it.src + 2]};
+        const float r3[3] = {pos_rcv[3 * it.rcv], pos_rcv[3 * it.rcv + 1], pos_rcv[3 * it.rcv + 2]};
+        m = images_miss_segment(R.L, R.nb, s3, r3, R.kh, R.H, it.t_lo, it.t_hi) ? 1 : 0;
+    }
+    skip[k] = m;
+}
+
+cudaError_t item_skip_launch(const RoomDesc *rooms, const IsmItem *items, int n_items, const float *pos_src,
+                             const float *pos_rcv, unsigned char *skip, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    item_skip_kernel<<<(n_items + 255) / 256, 256, 0, st>>>(rooms, items, n_items, pos_src, pos_rcv, skip);
+    return cudaGetLastError();
 }
 
 // Sum of the partial segments of each group, parts in increasing order (the result

@@ -25,7 +25,7 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
                                const float *orv_rcv, float *out, int *work_counter, int *status,
                                int em, int max_nsub, int clamp, int grid, cudaStream_t st, int mode,
                                int tw, const TailArgs *tail, float4 *axis_tab, int axis_cap,
-                               float *partial);
+                               float *partial, const unsigned char *skip);
 int describe_room(RoomDesc &R, const float room[3], const float beta[6], const int nb[3], float Tdiff,
                   float Tmax, float Fs, float c, int spkr, int mic);
 int window_plan(float H, int &tpl, int &em, int &clamp, int &max_nsub);
@@ -158,7 +158,8 @@ extern "C" int gpurir_simulate_ism_noalloc(const float room_sz[3], const float b
     if (cudaGetLastError() != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: prepare launch failed");
     if (ism_forward_launch(tpl, d_room, d_items, (int)n_items, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
-                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st, 0, tw, nullptr, nullptr, 0, nullptr) != cudaSuccess)
+                           d_rir_out, ctl, ctl + 1, em, nsub, clamp, grid, st, 0, tw, nullptr, nullptr, 0, nullptr,
+                           nullptr) != cudaSuccess)
         return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: kernel launch failed");
     return GPURIR_OK;
 }

@@ -5,7 +5,8 @@
 // Per room: beta, the Sabine T60 of src/gpuRIR_cuda.cu:123-130 in float32 (as the
 // reference and the host path evaluate it), and the power tables
 // pw[w][k] = (-beta_w)^k, k < pow_n, formed in FP64 by repeated multiplication and
-// rounded to float32, exactly as the host builds them (the same bits).
+// rounded to float32, exactly as the host builds them (the same bits); the serial
+// chain stops at pow_n, the entries after it are zero from the host's descriptor.
 #include "gpurir_internal.cuh"
 
 namespace gpurir {
@@ -19,9 +20,10 @@ __global__ void room_beta_kernel(RoomDesc *rooms, int n_rooms, const float *beta
         const float b = beta[6 * r + w];
         R.beta[w] = b;
         const double m = -(double)b;
+        const int n = R.pow_n;   // entries from pow_n on stay the zeros the host wrote
         double p = 1.0;
-        for (int k = 0; k < kPowMax; k++) {
-            R.pw[w][k] = k < R.pow_n ? (float)p : 0.0f;
+        for (int k = 0; k < n; k++) {
+            R.pw[w][k] = (float)p;
             p *= m;
         }
     }

@@ -244,3 +244,18 @@ def test_gradients_with_rirs_split_by_images(built):
     assert rel_l2(h.detach().cpu().numpy(), href) < 1e-5
     for k in ours:
         assert rel_l2(ours[k], ref[k]) < TOL, k
+
+
+def test_gradients_with_segments_past_the_images(built):
+    """A long RIR over a small image set: most segments lie past every image's window
+    and the adjoint skips them from the actual positions.  One source is outside the
+    room (its images reach beyond the in-room delay bound), so a wrong skip would lose
+    part of its gradient."""
+    c = _setup(37, "card", "omni", ns=2, nr=3, nb=(5, 6, 7), T=0.3)
+    c["ps"][1] = np.array([9.0, 1.5, 1.2], np.float32)
+    ours, h = _ours(c)
+    ref, href = _ref(c)
+    assert rel_l2(h.detach().cpu().numpy(), href) < 1e-5
+    for k in ours:
+        e = rel_l2(ours[k], ref[k])
+        assert e < TOL, (k, e)

@@ -265,3 +265,23 @@ def test_rirs_split_by_images_with_tail(built):
     n = p["n_ism"]
     assert np.all(p["A"] > 0)
     assert rel_l2(out[..., n:], ref[..., n:]) <= 1e-4
+
+
+def test_segments_past_the_last_image(built):
+    """A short image set in a long RIR: the planner cuts it into many segments, most of
+    them past every image's window; the device flags those from the actual positions.
+    One source lies outside the room (its images reach further than the in-room bound
+    the planner uses), so a wrong skip would drop its late images."""
+    rng = np.random.default_rng(11)
+    room = [3.0, 4.0, 2.5]
+    ps = np.concatenate([_rand_inside(rng, 1, room, 0.5), np.array([[9.5, 2.0, 1.0]], np.float32)])
+    pr = _rand_inside(rng, 2, room, 0.5)
+    out, ref, parts = _run(_sim(), room, [0.8] * 6, ps, pr, [5, 5, 5], 0.3, 16000.0)
+    n = parts["n_ism"]
+    _check_ism(out, ref, n, "segments past the images")
+    # the far source's windows reach past sample 900 (the in-room delay bound of this room
+    # is ~850 samples): that energy must be there, and everything after it is zero
+    late = slice(850, 1000)
+    assert np.abs(ref[1, :, late]).max() > 1e-4 * np.abs(ref).max()
+    assert np.abs(out[1, :, late] - ref[1, :, late]).max() <= 1e-5 * np.abs(ref).max()
+    assert not np.any(out[:, :, 1000:n])
