@@ -257,7 +257,7 @@ def _extra_inverse(workloads, sim, flush, stream, fs, dev):
             model(beta, ps, pr, None, orv)
 
     def fwd_bwd():
-        loss = ((model(beta, ps, pr, None, orv) - target) ** 2).sum()
+        loss = torch.nn.functional.mse_loss(model(beta, ps, pr, None, orv), target, reduction="sum")
         loss.backward()
 
     for _ in range(3):

@@ -36,7 +36,8 @@ class _IsmBatch(torch.autograd.Function):
         _lib.check(_lib.load().gpurir_adjoint_forward(
             batch.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
             out.data_ptr(), ctypes.c_void_p(st)), "gpurir_adjoint_forward")
-        ctx.batch = batch
+        batch._forwards += 1
+        ctx.batch, ctx.forward_no = batch, batch._forwards
         ctx.save_for_backward(beta, pos_src, pos_rcv, orV_src, orV_rcv)
         return out
 
@@ -53,8 +54,11 @@ class _IsmBatch(torch.autograd.Function):
         gor = torch.empty_like(orV_rcv) if orV_rcv is not None and ctx.needs_input_grad[4] else None
         ptr = lambda t: t.data_ptr() if t is not None else None
         st = torch.cuda.current_stream(dev).cuda_stream
+        # no forward call on this batch since ours: its room tables (from this beta, which
+        # autograd guarantees unmodified) are still on the device
+        beta_ptr = None if batch._forwards == ctx.forward_no else beta.data_ptr()
         _lib.check(_lib.load().gpurir_adjoint_backward(
-            batch.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
+            batch.handle, beta_ptr, ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
             g.data_ptr(), ptr(gb), ptr(gs), ptr(gr), ptr(gos), ptr(gor), ctypes.c_void_p(st)),
             "gpurir_adjoint_backward")
         return gb, gs, gr, gos, gor, None
@@ -75,6 +79,7 @@ class TorchBatch:
         self.offsets = layout(rooms, fs)
         self.total = int(self.offsets[-1])
         self.fs, self.c = fs, c
+        self._forwards = 0   # forward calls so far (the backward reuses the latest one's room tables)
         self.sim = sim or simulator()
         self._L = _lib.load()
         h = ctypes.c_void_p()

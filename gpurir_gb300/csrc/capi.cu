@@ -1062,17 +1062,26 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
             return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
     Plan P;
     if ((rc = plan_rooms(s, R, P))) return rc;
-    const int n_items = (int)P.items.size();
     int max_tseg = 1;
     for (const IsmItem &it : P.items) max_tseg = std::max(max_tseg, it.t_hi - it.t_lo);
+    const int pad = 64 * P.tpl;
+    const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad);
+    int bps = 0;
+    if (!P.items.empty()) {
+        if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
+        bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, smem);
+        if (bps < 1) return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
+    }
+    const std::vector<IsmItem> &bi = P.items;
+    const int n_items = (int)bi.size();
     std::vector<int> p_room, l_room, p_src, l_src, p_rcv, l_rcv;
-    csr(P.items, n_rooms, &IsmItem::room, 0, p_room, l_room);
-    csr(P.items, (int)ns, &IsmItem::src, 0, p_src, l_src);
-    csr(P.items, (int)nr, &IsmItem::rcv, 0, p_rcv, l_rcv);
+    csr(bi, n_rooms, &IsmItem::room, 0, p_room, l_room);
+    csr(bi, (int)ns, &IsmItem::src, 0, p_src, l_src);
+    csr(bi, (int)nr, &IsmItem::rcv, 0, p_rcv, l_rcv);
     // staging: rooms | items | csr arrays ; device adds item partials
     size_t o_rooms = 0;
     size_t o_items = align_up(R.size() * sizeof(RoomDesc), 256);
-    size_t o_csr = align_up(o_items + P.items.size() * sizeof(IsmItem), 256);
+    size_t o_csr = align_up(o_items + bi.size() * sizeof(IsmItem), 256);
     const std::vector<int> *arrs[6] = {&p_room, &l_room, &p_src, &l_src, &p_rcv, &l_rcv};
     size_t o_arr[6], off = o_csr;
     for (int a = 0; a < 6; a++) { o_arr[a] = off; off = align_up(off + arrs[a]->size() * sizeof(int), 256); }
@@ -1083,7 +1092,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     if ((rc = ensure_stage(s, stage_bytes))) return rc;
     char *h = s->h_stage;
     memcpy(h + o_rooms, R.data(), R.size() * sizeof(RoomDesc));
-    if (n_items) memcpy(h + o_items, P.items.data(), P.items.size() * sizeof(IsmItem));
+    if (n_items) memcpy(h + o_items, bi.data(), bi.size() * sizeof(IsmItem));
     for (int a = 0; a < 6; a++)
         if (!arrs[a]->empty()) memcpy(h + o_arr[a], arrs[a]->data(), arrs[a]->size() * sizeof(int));
     char *d = s->d_ws;
@@ -1096,11 +1105,6 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     if (n_items == 0) {
         CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));
     } else {
-        const int pad = 64 * P.tpl;
-        const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad);
-        if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
-        const int bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, smem);
-        if (bps < 1) return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
         const int grid = std::min(n_items, s->num_sms * bps);
         CK(ism_backward_launch(P.tpl, reinterpret_cast<const RoomDesc *>(d + o_rooms),
                                reinterpret_cast<const IsmItem *>(d + o_items), n_items, d_pos_src,
@@ -1131,6 +1135,7 @@ struct gpurir_adjoint {
     long long out_elems = 0;
     int max_tseg = 1, grid_b = 0;
     bool need_orv_src = false, need_orv_rcv = false;
+    bool rooms_written = false;   // a forward call has written the room tables
     size_t o_arr[6] = {}, o_ig = 0, o_ctl = 0;
 };
 
@@ -1159,20 +1164,21 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
     const Plan &P = a->P;
     a->M = (long)P.rirs.size();
     a->L = make_layout(P, R.size(), a->ns, a->nr, a->M, a->out_elems, false);
-    const int n_items = (int)P.items.size();
     for (const IsmItem &it : P.items) a->max_tseg = std::max(a->max_tseg, it.t_hi - it.t_lo);
-    if (n_items > 0 && ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl) > 227 * 1024) {
+    if (!P.items.empty() && ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl) > 227 * 1024) {
         delete a;
         return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
     }
-    if (n_items > 0) {
-        const int bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl));
+    int bps = 0;
+    if (!P.items.empty()) {
+        bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl));
         if (bps < 1) {
             delete a;
             return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
         }
-        a->grid_b = std::min(n_items, s->num_sms * bps);
     }
+    const int n_items = (int)P.items.size();
+    a->grid_b = std::min(n_items, s->num_sms * bps);
     std::vector<int> lists[6];
     csr(P.items, n_rooms, &IsmItem::room, 0, lists[0], lists[1]);
     csr(P.items, (int)a->ns, &IsmItem::src, 0, lists[2], lists[3]);
@@ -1208,6 +1214,7 @@ extern "C" int gpurir_adjoint_forward(gpurir_adjoint *a, const float *d_beta, co
     int *ctl = reinterpret_cast<int *>(a->d + a->o_ctl);
     uint64_t *offset = reinterpret_cast<uint64_t *>(a->d + a->o_ctl + 16);
     CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
+    a->rooms_written = true;
     int rc = enqueue_kernels(a->sim, a->P, a->d, a->L, a->M, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
                              d_out, ctl, offset, st, false);
     if (rc) return rc;
@@ -1220,7 +1227,9 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
                                        const float *d_orV_rcv, const float *d_grad_rir, float *d_grad_beta,
                                        float *d_grad_pos_src, float *d_grad_pos_rcv, float *d_grad_orV_src,
                                        float *d_grad_orV_rcv, void *stream) {
-    if (!a || !d_beta || !d_pos_src || !d_pos_rcv || !d_grad_rir) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if (!a || !d_pos_src || !d_pos_rcv || !d_grad_rir) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if (!d_beta && !a->rooms_written)
+        return fail(GPURIR_ERR_INVALID, "d_beta is NULL but no forward call has written the room tables");
     if ((a->need_orv_src && !d_orV_src) || (a->need_orv_rcv && !d_orV_rcv))
         return fail(GPURIR_ERR_INVALID, "orientation required for a non-omni pattern");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -1229,7 +1238,7 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
     const int n_items = (int)P.items.size();
     float *ig = reinterpret_cast<float *>(a->d + a->o_ig);
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(a->d + a->L.o_rooms);
-    CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
+    if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
     if (n_items == 0) {
         CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));
     } else {

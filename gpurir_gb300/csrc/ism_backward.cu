@@ -22,10 +22,8 @@
 
 namespace gpurir {
 
-constexpr int kBThreads = 256;   // two blocks per SM (registers): one block's barriers overlap the other's work
+constexpr int kBThreads = 256;   // three blocks per SM (registers)
 constexpr int kBWarps = kBThreads / 32;
-constexpr int kBChunk = 512;
-constexpr int kBRounds = kBChunk / kBThreads;   // images per lane and chunk
 constexpr int kGrad = 18;                       // beta[6], src[3], rcv[3], orv_src[3], orv_rcv[3]
 
 struct BwdLaunch {
@@ -47,6 +45,14 @@ __device__ __forceinline__ float rcp_approx_b(float x) {
     return r;
 }
 
+// Asynchronous 4-byte copy global -> shared; src_bytes = 0 writes a zero instead of
+// reading (PTX cp.async with a source size).
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Derivative of the polar-pattern gain with respect to cos(theta)
 // (src/gpuRIR_cuda.cu:140-145; homni is flat almost everywhere).
 __device__ __forceinline__ float pattern_slope(int pattern) {
@@ -60,20 +66,18 @@ __device__ __forceinline__ float pattern_slope(int pattern) {
 }
 
 template <int TPL, bool CLAMP>
-__global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P) {
-    constexpr int KS = 32 * TPL;
+__global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P) {
+    // per-warp scratch of 32 kept images: records, then A and B of each
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *rec = reinterpret_cast<float4 *>(smem_raw);          // sigma, f, cos phi, sin phi
-    float *rec_gamma = reinterpret_cast<float *>(rec + kBChunk);  // cos(pi f)
-    int *rec_n0 = reinterpret_cast<int *>(rec_gamma + kBChunk);   // floor(tau) - t_lo
-    int *rec_idx = rec_n0 + kBChunk;                              // image index
-    float *ga = reinterpret_cast<float *>(rec_idx + kBChunk);     // A per kept image
-    float *gb = ga + kBChunk;                                     // B per kept image
-    int *wcount = reinterpret_cast<int *>(gb + kBChunk);          // [kBWarps] kept per warp
-    int *woff = wcount + kBWarps;
-    int *ctl = woff + kBWarps;                                    // [0] item, [1] kept total
-    float *red = reinterpret_cast<float *>(ctl + 4);              // [kBWarps][kGrad]
-    float *gs = red + kBWarps * kGrad;                            // staged dL/dh
+    float4 *rec = reinterpret_cast<float4 *>(smem_raw);             // sigma, f, cos phi, sin phi
+    float *rec_gamma = reinterpret_cast<float *>(rec + kBThreads);   // cos(pi f)
+    int *rec_n0 = reinterpret_cast<int *>(rec_gamma + kBThreads);    // floor(tau) - t_lo
+    float *ga = reinterpret_cast<float *>(rec_n0 + kBThreads);       // A per kept image
+    float *gb = ga + kBThreads;                                      // B per kept image
+    int *ctl = reinterpret_cast<int *>(gb + kBThreads);              // [0] item
+    float *red = reinterpret_cast<float *>(ctl + 4);                 // [kBWarps][kGrad]
+    // then [kGrad][kBThreads] per-thread gradient partials
+    float *gs = red + (kBWarps + kBThreads) * kGrad;                 // staged dL/dh
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (;;) {
@@ -118,18 +122,20 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
             const float Lr[3] = {L0, L1, L2}, s3[3] = {sx, sy, sz}, r3[3] = {rx, ry, rz};
             miss = images_miss_segment(Lr, R.nb, s3, r3, R.kh, H, t_lo, t_hi);
         }
-        // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment.
+        // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment: copies
+        // in flight while the first images' geometry is computed
         if (!miss) {
             const int g_len = t_hi - t_lo + 2 * P.pad;
             const float *grow = P.grad + it.out_row;
             for (int i = tid; i < g_len; i += kBThreads) {
                 const int t = t_lo - P.pad + i;
-                gs[i] = (t >= t_lo && t < t_hi) ? grow[t] : 0.0f;
+                const bool in = t >= t_lo && t < t_hi;
+                cp_async4(gs + i, grow + (in ? t : t_lo), in ? 4 : 0);
             }
         }
         const float dws = 3.14159265358979323846f * inv_h;   // 2 pi / Tw
         // per-lane tap constants
-        float kf[TPL], ck[TPL], sk[TPL], ckd[TPL], skd[TPL];   // ckd, skd: times 2 pi / Tw
+        float kf[TPL], ck[TPL], sk[TPL];
 #pragma unroll
         for (int i = 0; i < TPL; i++) {
             kf[i] = (float)(k_lo + lane + 32 * i);
@@ -137,159 +143,138 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
             sincospif(kf[i] * inv_h, &sn, &cs);
             ck[i] = 0.5f * cs;
             sk[i] = 0.5f * sn;
-            ckd[i] = dws * ck[i];
-            skd[i] = dws * sk[i];
         }
         const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
-        float acc[kGrad];
+        // this thread's gradient partials of the item, in shared memory (registers go to
+        // the taps): acc(q) = accs[q * kBThreads + tid]
+        float *accs = red + kBWarps * kGrad;
+#define acc(q) accs[(q) * kBThreads + tid]
 #pragma unroll
-        for (int q = 0; q < kGrad; q++) acc[q] = 0.0f;
+        for (int q = 0; q < kGrad; q++) acc(q) = 0.0f;
 
         const int i_end = miss ? it.i_lo : min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
-        for (int cbase = it.i_lo; cbase < i_end; cbase += kBChunk) {
-            // ---- pass A: geometry, keep images whose window meets the segment (image order)
-            int kept_mine = 0;
-            int keep_flag[kBRounds];
-            float4 r4[kBRounds];
-            float rg[kBRounds];
-            int rn0[kBRounds], ridx[kBRounds];
-#pragma unroll
-            for (int r = 0; r < kBRounds; r++) {
-                const int local = warp * (32 * kBRounds) + r * 32 + lane;
-                const int i = cbase + local;
-                keep_flag[r] = 0;
-                r4[r] = make_float4(0.f, 0.f, 1.f, 0.f);
-                rg[r] = 1.f;
-                rn0[r] = 0;
-                ridx[r] = i;
-                if (i < i_end) {
-                    int q, m2, m0, m1;
-                    divmod_small(i, N2, rN2, q, m2);
-                    divmod_small(q, N1, rN1, m0, m1);
-                    int c0, r0, c1, r1, c2, r2;
-                    image_axis(m0, N0, c0, r0);
-                    image_axis(m1, N1, c1, r1);
-                    image_axis(m2, N2, c2, r2);
-                    const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
-                    const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
-                    const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
-                    const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
-                    // approximate distance first: far images stop here
-                    const float rs0 = rsqrtf(d2.hi);
-                    const float s0 = d2.hi * rs0;
-                    const float tau_est = s0 * kfs.hi;
-                    ff tau = {-1e30f, 0.0f};   // culled: fails the keep test below
-                    if (tau_est > keep_lo - 1.0f && tau_est < keep_hi + 1.0f) {
-                        float inv_d;
-                        tau = ff_mul(ff_dist_newton(d2, rs0, s0, inv_d), kfs);
-                    }
-                    if (tau.hi > keep_lo && tau.hi < keep_hi) {
-                        float fl = floorf(tau.hi);
-                        int n0 = (int)fl;
-                        float f = __fadd_rn(__fsub_rn(tau.hi, fl), tau.lo);
-                        if (f < 0.0f) { n0 -= 1; f += 1.0f; }
-                        if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
-                        f = fmaxf(f, 9.094947017729282e-13f);
-                        float sp, cp, sphi, cphi;
-                        sincospi_unit(f, sp, cp);
-                        if (small_phi) sincospi_small(f * inv_h, sphi, cphi);
-                        else sincospif(f * inv_h, &sphi, &cphi);
-                        r4[r] = make_float4(-sp * 0.318309886183790672f, f, cphi, sphi);
-                        rg[r] = cp;
-                        rn0[r] = n0 - t_lo;
-                        keep_flag[r] = 1;
-                        kept_mine++;
-                    }
+        // Each warp walks its own groups of 32 consecutive images (group g of the item goes
+        // to warp g mod kBWarps): geometry one image per lane, the kept images' records
+        // packed in the warp's scratch, their taps four images at a time over the lanes,
+        // then the chain rule one image per lane.  No block barrier inside an item.
+        float4 *wrec = rec + warp * 32;
+        float *wgam = rec_gamma + warp * 32;
+        int *wn0 = rec_n0 + warp * 32;
+        float *wga = ga + warp * 32, *wgb = gb + warp * 32;
+        bool keep = false;
+        float4 r4 = make_float4(0.f, 0.f, 1.f, 0.f);
+        float rg = 1.f;
+        int rn0 = 0;
+        // geometry of image ii: keep, (sigma, f, cos phi, sin phi), cos(pi f), n0 - t_lo
+        auto geometry = [&](const int ii) {
+            keep = false;
+            r4 = make_float4(0.f, 0.f, 1.f, 0.f);
+            rg = 1.f;
+            rn0 = 0;
+            if (ii < i_end) {
+                int q, m2, m0, m1;
+                divmod_small(ii, N2, rN2, q, m2);
+                divmod_small(q, N1, rN1, m0, m1);
+                int c0, r0, c1, r1, c2, r2;
+                image_axis(m0, N0, c0, r0);
+                image_axis(m1, N1, c1, r1);
+                image_axis(m2, N2, c2, r2);
+                const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
+                const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
+                const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
+                const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
+                // approximate distance first: far images stop here
+                const float rs0 = rsqrtf(d2.hi);
+                const float s0 = d2.hi * rs0;
+                const float tau_est = s0 * kfs.hi;
+                ff tau = {-1e30f, 0.0f};   // culled: fails the keep test below
+                if (tau_est > keep_lo - 1.0f && tau_est < keep_hi + 1.0f) {
+                    float inv_d;
+                    tau = ff_mul(ff_dist_newton(d2, rs0, s0, inv_d), kfs);
+                }
+                if (tau.hi > keep_lo && tau.hi < keep_hi) {
+                    float fl = floorf(tau.hi);
+                    int n0 = (int)fl;
+                    float f = __fadd_rn(__fsub_rn(tau.hi, fl), tau.lo);
+                    if (f < 0.0f) { n0 -= 1; f += 1.0f; }
+                    if (f >= 1.0f) { n0 += 1; f -= 1.0f; }
+                    f = fmaxf(f, 9.094947017729282e-13f);
+                    float sp, cp, sphi, cphi;
+                    sincospi_unit(f, sp, cp);
+                    if (small_phi) sincospi_small(f * inv_h, sphi, cphi);
+                    else sincospif(f * inv_h, &sphi, &cphi);
+                    r4 = make_float4(-sp * 0.318309886183790672f, f, cphi, sphi);
+                    rg = cp;
+                    rn0 = n0 - t_lo;
+                    keep = true;
                 }
             }
-            // warp-level compaction in image order
-            int wsum = 0, my_before = 0;
-            unsigned bal[kBRounds];
-#pragma unroll
-            for (int r = 0; r < kBRounds; r++) {
-                bal[r] = __ballot_sync(0xffffffffu, keep_flag[r]);
-                wsum += __popc(bal[r]);
+        };
+        int gbase = it.i_lo + warp * 32;
+        geometry(gbase + lane);
+        cp_async_wait_all();
+        __syncthreads();   // g staged
+        for (; gbase < i_end; gbase += kBThreads) {
+            const int i = gbase + lane;
+            const unsigned kmask = __ballot_sync(0xffffffffu, keep);
+            const int n_k = __popc(kmask);
+            const int slot = __popc(kmask & ((1u << lane) - 1u));
+            if (keep) {
+                wrec[slot] = r4;
+                wgam[slot] = rg;
+                wn0[slot] = rn0;
             }
-            if (lane == 0) wcount[warp] = wsum;
-            __syncthreads();
-            if (tid == 0) {
-                int run = 0;
-                for (int w = 0; w < kBWarps; w++) { woff[w] = run; run += wcount[w]; }
-                ctl[1] = run;
-            }
-            __syncthreads();
-            {
-                int pos = woff[warp];
+            __syncwarp();
+            // per kept image, A and B over its taps, four images per trip
+            const float *gl = gs + P.pad + lane;
+            for (int j = 0; j < n_k; j += 4) {
+                float v[8];
 #pragma unroll
-                for (int r = 0; r < kBRounds; r++) {
-                    if (keep_flag[r]) {
-                        const int j = pos + __popc(bal[r] & ((1u << lane) - 1u));
-                        rec[j] = r4[r];
-                        rec_gamma[j] = rg[r];
-                        rec_n0[j] = rn0[r];
-                        rec_idx[j] = ridx[r];
+                for (int u = 0; u < 4; u++) {
+                    const int jj = min(j + u, n_k - 1);
+                    const float4 c = wrec[jj];
+                    const float sig = c.x * lane_sign, f = c.y, cphi = c.z, sphi = c.w;
+                    const float cphd = dws * cphi, sphd = dws * sphi;   // w' = ck sphd - sk cphd
+                    const float gam = wgam[jj] * lane_sign;
+                    const float *gp = gl + wn0[jj] + k_lo;
+                    // sigma and gamma are constant over the image: with q = g / x,
+                    //   sum g W  = sigma S,   S = sum q w
+                    //   sum g W' = sigma T + gamma S,   T = sum q (w' - w / x)
+                    float s1 = 0.0f, t1 = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < TPL; k++) {
+                        const float x = kf[k] - f;
+                        const float rx_ = rcp_approx_b(x);
+                        const float w = fmaf(ck[k], cphi, fmaf(sk[k], sphi, 0.5f));
+                        const float wd = fmaf(ck[k], sphd, -sk[k] * cphd);
+                        float q = gp[32 * k] * rx_;
+                        if (CLAMP && fabsf(x) >= H) q = 0.0f;
+                        s1 = fmaf(q, w, s1);
+                        t1 = fmaf(q, fmaf(-w, rx_, wd), t1);
                     }
-                    pos += __popc(bal[r]);
+                    v[2 * u] = sig * s1;
+                    v[2 * u + 1] = fmaf(sig, t1, gam * s1);
                 }
-            }
-            (void)kept_mine;
-            __syncthreads();
-            const int n_kept = ctl[1];
-            // ---- pass B: per kept image, A and B over its taps; contiguous slices per warp
-            {
-                const int per = (n_kept + kBWarps - 1) / kBWarps;
-                const int j0 = min(warp * per, n_kept), j1 = min(j0 + per, n_kept);
-                const float *gl = gs + P.pad + lane;
-                for (int j = j0; j < j1; j += 2) {
-                    float a[2] = {0.f, 0.f}, b[2] = {0.f, 0.f};
+                // reduce the 8 values over the warp with 9 shuffles: afterwards lanes 4m..4m+3
+                // hold value m = 2 u + (0: A, 1: B) of image j + u
+                const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+                float w4[4], w2[2];
 #pragma unroll
-                    for (int u = 0; u < 2; u++) {
-                        const int jj = min(j + u, j1 - 1);
-                        const float4 c = rec[jj];
-                        const float sig = c.x * lane_sign, f = c.y, cphi = c.z, sphi = c.w;
-                        const float gam = rec_gamma[jj] * lane_sign;
-                        const float *gp = gl + rec_n0[jj] + k_lo;
-                        // sigma and gamma are constant over the image: with q = g / x,
-                        //   sum g W  = sigma S,   S = sum q w
-                        //   sum g W' = sigma T + gamma S,   T = sum q (w' - w / x)
-                        float s1 = 0.0f, t1 = 0.0f;
+                for (int e = 0; e < 4; e++)
+                    w4[e] = (b4 ? v[4 + e] : v[e]) + __shfl_xor_sync(0xffffffffu, b4 ? v[e] : v[4 + e], 16);
 #pragma unroll
-                        for (int i = 0; i < TPL; i++) {
-                            const float x = kf[i] - f;
-                            const float rx_ = rcp_approx_b(x);
-                            const float w = fmaf(ck[i], cphi, fmaf(sk[i], sphi, 0.5f));
-                            const float wd = fmaf(ckd[i], sphi, -skd[i] * cphi);
-                            float q = gp[32 * i] * rx_;
-                            if (CLAMP && fabsf(x) >= H) q = 0.0f;
-                            s1 = fmaf(q, w, s1);
-                            t1 = fmaf(q, fmaf(-w, rx_, wd), t1);
-                        }
-                        a[u] = sig * s1;
-                        b[u] = fmaf(sig, t1, gam * s1);
-                    }
-                    if (j + 1 >= j1) { a[1] = 0.f; b[1] = 0.f; }
-                    // reduce 4 values over the warp with 6 shuffles
-                    const bool hi = lane & 16;
-                    float x0 = (hi ? a[1] : a[0]) + __shfl_xor_sync(0xffffffffu, hi ? a[0] : a[1], 16);
-                    float x1 = (hi ? b[1] : b[0]) + __shfl_xor_sync(0xffffffffu, hi ? b[0] : b[1], 16);
-                    const bool b3 = lane & 8;
-                    float y = (b3 ? x1 : x0) + __shfl_xor_sync(0xffffffffu, b3 ? x0 : x1, 8);
-                    y += __shfl_xor_sync(0xffffffffu, y, 4);
-                    y += __shfl_xor_sync(0xffffffffu, y, 2);
-                    y += __shfl_xor_sync(0xffffffffu, y, 1);
-                    // lanes 0 / 8 / 16 / 24 hold A(j) / B(j) / A(j+1) / B(j+1)
-                    if (lane == 0) ga[j] = y;
-                    if (lane == 8) gb[j] = y;
-                    if (j + 1 < j1) {
-                        if (lane == 16) ga[j + 1] = y;
-                        if (lane == 24) gb[j + 1] = y;
-                    }
-                }
+                for (int e = 0; e < 2; e++)
+                    w2[e] = (b3 ? w4[2 + e] : w4[e]) + __shfl_xor_sync(0xffffffffu, b3 ? w4[e] : w4[2 + e], 8);
+                float y = (b2 ? w2[1] : w2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? w2[0] : w2[1], 4);
+                y += __shfl_xor_sync(0xffffffffu, y, 2);
+                y += __shfl_xor_sync(0xffffffffu, y, 1);
+                const int m = lane >> 2, u = m >> 1;
+                if ((lane & 3) == 0 && j + u < n_k) (m & 1 ? wgb : wga)[j + u] = y;
             }
-            __syncthreads();
-            // ---- pass C: chain rule, one kept image per lane
-            for (int j = tid; j < n_kept; j += kBThreads) {
-                const int i = rec_idx[j];
+            __syncwarp();
+            // chain rule, one kept image per lane
+            if (keep) {
+                const int j = slot;
                 int q, m2, m0, m1;
                 divmod_small(i, N2, rN2, q, m2);
                 divmod_small(q, N1, rN1, m0, m1);
@@ -326,8 +311,8 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
                 }
                 const float g0 = 0.0795774715459476679f * inv_d;   // 1 / (4 pi d)
                 const float amp = att * Ds * Dm * g0;
-                const float GA = ga[j];
-                const float GT = -amp * gb[j];                      // dL/dtau
+                const float GA = wga[j];
+                const float GT = -amp * wgb[j];                      // dL/dtau
                 // beta: d att / d beta_w = -e_w (-beta_w)^(e_w - 1) * (other five factors)
 #pragma unroll
                 for (int w = 0; w < 6; w++) {
@@ -337,7 +322,7 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
                         for (int u = 0; u < 6; u++)
                             if (u != w) others *= pwv[u];
                         const float datt = -(float)e[w] * __ldg(&R.pw[w][e[w] - 1]) * others;
-                        acc[w] = fmaf(GA * Ds * Dm * g0, datt, acc[w]);
+                        acc(w) = fmaf(GA * Ds * Dm * g0, datt, acc(w));
                     }
                 }
                 // d amp / d v and d tau / d v
@@ -355,30 +340,31 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
                 }
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    acc[6 + d] += rr[d] ? -dv[d] : dv[d];   // source: image coordinate (1 - 2 refl) src
-                    acc[9 + d] -= dv[d];                    // receiver
+                    acc(6 + d) += rr[d] ? -dv[d] : dv[d];   // source: image coordinate (1 - 2 refl) src
+                    acc(9 + d) -= dv[d];                    // receiver
                 }
                 if (spkr != P_OMNI) {   // d cos_s / d o = (-(1-2r) v / d - cos_s o / |o|) / |o|
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         const float dcs = (-(rr[d] ? -v[d] : v[d]) * inv_d - cs_ * os[d] * inv_os) * inv_os;
-                        acc[12 + d] = fmaf(GA * att * g0 * Dm * ds, dcs, acc[12 + d]);
+                        acc(12 + d) = fmaf(GA * att * g0 * Dm * ds, dcs, acc(12 + d));
                     }
                 }
                 if (mic != P_OMNI) {    // d cos_m / d o = (v / d - cos_m o / |o|) / |o|
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         const float dcm = (v[d] * inv_d - cm * orr[d] * inv_or) * inv_or;
-                        acc[15 + d] = fmaf(GA * att * g0 * Ds * dm, dcm, acc[15 + d]);
+                        acc(15 + d) = fmaf(GA * att * g0 * Ds * dm, dcm, acc(15 + d));
                     }
                 }
             }
-            __syncthreads();
+            __syncwarp();   // the scratch is rewritten by the next group
+            if (gbase + kBThreads < i_end) geometry(gbase + kBThreads + lane);
         }
         // ---- item partials: warp sums, then warps in order
 #pragma unroll
         for (int q = 0; q < kGrad; q++) {
-            float v = acc[q];
+            float v = acc(q);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0) red[warp * kGrad + q] = v;
@@ -391,6 +377,7 @@ __global__ void __launch_bounds__(kBThreads, 2) ism_backward_kernel(BwdLaunch P)
         }
         __syncthreads();
     }
+#undef acc
 }
 
 // Sum of item partials per target: one warp per target of the five sets (rooms:
@@ -431,8 +418,8 @@ __global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
 
 size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
     (void)tpl;
-    return kBChunk * (sizeof(float4) + 5 * sizeof(int)) + (2 * kBWarps + 4) * sizeof(int) +
-           kBWarps * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
+    return kBThreads * (sizeof(float4) + 4 * sizeof(int)) + 4 * sizeof(int) +
+           (kBWarps + kBThreads) * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
 }
 
 template <int TPL, bool CLAMP>

@@ -176,8 +176,11 @@ int gpurir_ism_backward_batch_device_beta(gpurir_sim *sim, int n_rooms, const gp
  * synchronisation, no allocation), reading the wall coefficients from d_beta
  * [n_rooms][6] at every call, so a whole step (forward, loss, adjoint) can be
  * recorded in a CUDA graph.  Arguments as gpurir_simulate_batch_device_beta and
- * gpurir_ism_backward_batch_device_beta.  gpurir_adjoint_status returns the
- * kernels' error word (0: none).  No counterpart in the reference. */
+ * gpurir_ism_backward_batch_device_beta, except that gpurir_adjoint_backward takes
+ * d_beta = NULL to reuse the room tables of the last gpurir_adjoint_forward on the
+ * same handle (stream-ordered after it, with the same coefficients: one launch less
+ * per step).  gpurir_adjoint_status returns the kernels' error word (0: none).
+ * No counterpart in the reference. */
 typedef struct gpurir_adjoint gpurir_adjoint;
 int gpurir_adjoint_create(gpurir_sim *sim, int n_rooms, const gpurir_room *rooms, float Fs, float c,
                           gpurir_adjoint **out);

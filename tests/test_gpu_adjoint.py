@@ -259,3 +259,36 @@ def test_gradients_with_segments_past_the_images(built):
     for k in ours:
         e = rel_l2(ours[k], ref[k])
         assert e < TOL, (k, e)
+
+
+def test_backward_after_two_forwards_uses_each_calls_beta(built):
+    """The backward reuses the room tables of the forward only when no other forward
+    ran on the batch in between: two calls with different beta, then one backward,
+    give the same gradients as the two calls differentiated one at a time."""
+    import torch
+    from gpurir_gb300.autograd import TorchBatch
+    c = _setup(41, "omni", "card", ns=1, nr=2, nb=(5, 5, 5), T=0.05)
+    room = dict(room_sz=c["room"], beta=c["beta"], pos_src=c["ps"], pos_rcv=c["pr"], nb_img=c["nb"],
+                Tmax=c["T"], Tdiff=c["T"], spkr_pattern="omni", mic_pattern="card")
+    model = TorchBatch([room], 16000.0)
+    rng = np.random.default_rng(5)
+    b1 = torch.tensor(c["beta"][None], device="cuda")
+    b2 = torch.tensor(np.clip(c["beta"][None] - 0.1, 0.0, 1.0), device="cuda")
+    ps, pr = torch.tensor(c["ps"], device="cuda"), torch.tensor(c["pr"], device="cuda")
+    orv = torch.tensor(c["orv"], device="cuda")
+    g1 = torch.tensor(rng.standard_normal(model.total), dtype=torch.float32, device="cuda")
+    g2 = torch.tensor(rng.standard_normal(model.total), dtype=torch.float32, device="cuda")
+
+    def grads(pairs):
+        out = []
+        for b, g in pairs:
+            x = b.clone().requires_grad_(True)
+            out.append((x, (model(x, ps, pr, None, orv) * g).sum()))
+        sum(l for _, l in out).backward()
+        return [x.grad.cpu().numpy() for x, _ in out]
+
+    both = grads([(b1, g1), (b2, g2)])
+    one1, = grads([(b1, g1)])
+    one2, = grads([(b2, g2)])
+    assert np.array_equal(both[0], one1) and np.array_equal(both[1], one2)
+    assert not np.allclose(one1, one2)
