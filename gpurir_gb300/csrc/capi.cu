@@ -60,6 +60,9 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
                        int L, long n_out, double *out, cudaStream_t st);
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
+cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
+                                  int n_items, const float *pos_src, const float *pos_rcv, unsigned char *skip,
+                                  cudaStream_t st);
 }  // namespace gpurir
 
 using namespace gpurir;
@@ -568,7 +571,7 @@ static void fill_stage(char *h, const Layout &L, const std::vector<RoomDesc> &R,
 static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const Layout &L, long M,
                            const float *dps, const float *dpr, const float *dos, const float *dor,
                            float *dout, int *work_counter, const uint64_t *offset_ptr,
-                           cudaStream_t st, bool record) {
+                           cudaStream_t st, bool record, bool skip_ready = false) {
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + L.o_rooms);
     if (record && s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
     TailArgs ta;
@@ -582,9 +585,11 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     unsigned char *skip = nullptr;
     if (P.grid > 0 && P.skip_flags) {   // segments no image may reach: flags at the current positions
         skip = reinterpret_cast<unsigned char *>(const_cast<char *>(d) + L.o_skip);
-        CK(item_skip_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_items), (int)P.items.size(),
-                            dps, dpr, skip, st));
-        if (record) s->last_launches += 1;
+        if (!skip_ready) {   // (else written by room_beta_skip_kernel just before)
+            CK(item_skip_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_items), (int)P.items.size(),
+                                dps, dpr, skip, st));
+            if (record) s->last_launches += 1;
+        }
     }
     if (P.grid > 0)
         CK(ism_forward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(d + L.o_items),
@@ -1213,10 +1218,16 @@ extern "C" int gpurir_adjoint_forward(gpurir_adjoint *a, const float *d_beta, co
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     int *ctl = reinterpret_cast<int *>(a->d + a->o_ctl);
     uint64_t *offset = reinterpret_cast<uint64_t *>(a->d + a->o_ctl + 16);
-    CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
+    const bool fuse_skip = a->P.grid > 0 && a->P.skip_flags;
+    if (fuse_skip)   // room tables and the items' skip flags in one launch
+        CK(room_beta_skip_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta,
+                                 reinterpret_cast<const IsmItem *>(a->d + a->L.o_items), (int)a->P.items.size(),
+                                 d_pos_src, d_pos_rcv, reinterpret_cast<unsigned char *>(a->d + a->L.o_skip), st));
+    else
+        CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
     a->rooms_written = true;
     int rc = enqueue_kernels(a->sim, a->P, a->d, a->L, a->M, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv,
-                             d_out, ctl, offset, st, false);
+                             d_out, ctl, offset, st, false, fuse_skip);
     if (rc) return rc;
     if (a->P.max_n_diff > 0) CK(advance_counter_launch(offset, st));   // the next call draws new noise
     return GPURIR_OK;

@@ -69,10 +69,11 @@ template <int TPL, bool CLAMP>
 __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P) {
     // per-warp scratch of 32 kept images: records, then A and B of each
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *rec = reinterpret_cast<float4 *>(smem_raw);             // sigma, f, cos phi, sin phi
-    float *rec_gamma = reinterpret_cast<float *>(rec + kBThreads);   // cos(pi f)
-    int *rec_n0 = reinterpret_cast<int *>(rec_gamma + kBThreads);    // floor(tau) - t_lo
-    float *ga = reinterpret_cast<float *>(rec_n0 + kBThreads);       // A per kept image
+    // records of the kept images: (sigma, f, cos phi, sin phi) and
+    // (2 pi/Tw cos phi, 2 pi/Tw sin phi, cos(pi f), floor(tau) - t_lo as int bits)
+    float4 *rec = reinterpret_cast<float4 *>(smem_raw);
+    float4 *rec2 = rec + kBThreads;
+    float *ga = reinterpret_cast<float *>(rec2 + kBThreads);         // A per kept image
     float *gb = ga + kBThreads;                                      // B per kept image
     int *ctl = reinterpret_cast<int *>(gb + kBThreads);              // [0] item
     float *red = reinterpret_cast<float *>(ctl + 4);                 // [kBWarps][kGrad]
@@ -80,6 +81,23 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
     float *gs = red + (kBWarps + kBThreads) * kGrad;                 // staged dL/dh
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // per-lane tap constants; one Fs per launch, so one window for every room: computed
+    // once per block
+    float kf[TPL], ck[TPL], sk[TPL];
+    {
+        const float H0 = P.rooms[0].H, inv_h0 = 1.0f / H0;
+        const int k_lo0 = (int)floorf(-H0) + 1;
+#pragma unroll
+        for (int i = 0; i < TPL; i++) {
+            kf[i] = (float)(k_lo0 + lane + 32 * i);
+            float sn, cs;
+            sincospif(kf[i] * inv_h0, &sn, &cs);
+            // the lane's sign (-1)^k goes into the window constants
+            const float ls = ((k_lo0 + lane) & 1) ? -0.5f : 0.5f;
+            ck[i] = ls * cs;
+            sk[i] = ls * sn;
+        }
+    }
     for (;;) {
         if (tid == 0) ctl[0] = atomicAdd(P.work_counter, 1);
         __syncthreads();
@@ -122,9 +140,14 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
             const float Lr[3] = {L0, L1, L2}, s3[3] = {sx, sy, sz}, r3[3] = {rx, ry, rz};
             miss = images_miss_segment(Lr, R.nb, s3, r3, R.kh, H, t_lo, t_hi);
         }
+        if (miss) {   // zero partials, nothing else
+            if (tid < kGrad) P.item_grad[(long)item_id * kGrad + tid] = 0.0f;
+            __syncthreads();
+            continue;
+        }
         // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment: copies
         // in flight while the first images' geometry is computed
-        if (!miss) {
+        {
             const int g_len = t_hi - t_lo + 2 * P.pad;
             const float *grow = P.grad + it.out_row;
             for (int i = tid; i < g_len; i += kBThreads) {
@@ -134,17 +157,7 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
             }
         }
         const float dws = 3.14159265358979323846f * inv_h;   // 2 pi / Tw
-        // per-lane tap constants
-        float kf[TPL], ck[TPL], sk[TPL];
-#pragma unroll
-        for (int i = 0; i < TPL; i++) {
-            kf[i] = (float)(k_lo + lane + 32 * i);
-            float sn, cs;
-            sincospif(kf[i] * inv_h, &sn, &cs);
-            ck[i] = 0.5f * cs;
-            sk[i] = 0.5f * sn;
-        }
-        const float lane_sign = ((k_lo + lane) & 1) ? -1.0f : 1.0f;
+        const float half_sign = ((k_lo + lane) & 1) ? -0.5f : 0.5f;   // (-1)^k / 2
         // this thread's gradient partials of the item, in shared memory (registers go to
         // the taps): acc(q) = accs[q * kBThreads + tid]
         float *accs = red + kBWarps * kGrad;
@@ -152,14 +165,12 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
 #pragma unroll
         for (int q = 0; q < kGrad; q++) acc(q) = 0.0f;
 
-        const int i_end = miss ? it.i_lo : min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
+        const int i_end = min(it.i_hi, n_img);   // this item's images: [i_lo, i_end)
         // Each warp walks its own groups of 32 consecutive images (group g of the item goes
         // to warp g mod kBWarps): geometry one image per lane, the kept images' records
         // packed in the warp's scratch, their taps four images at a time over the lanes,
         // then the chain rule one image per lane.  No block barrier inside an item.
-        float4 *wrec = rec + warp * 32;
-        float *wgam = rec_gamma + warp * 32;
-        int *wn0 = rec_n0 + warp * 32;
+        float4 *wrec = rec + warp * 32, *wrec2 = rec2 + warp * 32;
         float *wga = ga + warp * 32, *wgb = gb + warp * 32;
         bool keep = false;
         float4 r4 = make_float4(0.f, 0.f, 1.f, 0.f);
@@ -221,8 +232,7 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
             const int slot = __popc(kmask & ((1u << lane) - 1u));
             if (keep) {
                 wrec[slot] = r4;
-                wgam[slot] = rg;
-                wn0[slot] = rn0;
+                wrec2[slot] = make_float4(dws * r4.z, dws * r4.w, rg, __int_as_float(rn0));
             }
             __syncwarp();
             // per kept image, A and B over its taps, four images per trip
@@ -232,12 +242,12 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const int jj = min(j + u, n_k - 1);
-                    const float4 c = wrec[jj];
-                    const float sig = c.x * lane_sign, f = c.y, cphi = c.z, sphi = c.w;
-                    const float cphd = dws * cphi, sphd = dws * sphi;   // w' = ck sphd - sk cphd
-                    const float gam = wgam[jj] * lane_sign;
-                    const float *gp = gl + wn0[jj] + k_lo;
-                    // sigma and gamma are constant over the image: with q = g / x,
+                    const float4 c = wrec[jj], c2 = wrec2[jj];
+                    const float sig = c.x, f = c.y, cphi = c.z, sphi = c.w;
+                    const float cphd = c2.x, sphd = c2.y, gam = c2.z;   // w' = ck sphd - sk cphd
+                    const float *gp = gl + __float_as_int(c2.w) + k_lo;
+                    // sigma and gamma are constant over the image: with q = g / x and the
+                    // lane's sign (-1)^k inside w and w',
                     //   sum g W  = sigma S,   S = sum q w
                     //   sum g W' = sigma T + gamma S,   T = sum q (w' - w / x)
                     float s1 = 0.0f, t1 = 0.0f;
@@ -245,7 +255,7 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
                     for (int k = 0; k < TPL; k++) {
                         const float x = kf[k] - f;
                         const float rx_ = rcp_approx_b(x);
-                        const float w = fmaf(ck[k], cphi, fmaf(sk[k], sphi, 0.5f));
+                        const float w = fmaf(ck[k], cphi, fmaf(sk[k], sphi, half_sign));
                         const float wd = fmaf(ck[k], sphd, -sk[k] * cphd);
                         float q = gp[32 * k] * rx_;
                         if (CLAMP && fabsf(x) >= H) q = 0.0f;
@@ -418,7 +428,7 @@ __global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
 
 size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
     (void)tpl;
-    return kBThreads * (sizeof(float4) + 4 * sizeof(int)) + 4 * sizeof(int) +
+    return kBThreads * (2 * sizeof(float4) + 2 * sizeof(float)) + 4 * sizeof(int) +
            (kBWarps + kBThreads) * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
 }
 

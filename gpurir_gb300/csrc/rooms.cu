@@ -11,9 +11,7 @@
 
 namespace gpurir {
 
-__global__ void room_beta_kernel(RoomDesc *rooms, int n_rooms, const float *beta) {
-    const int r = blockIdx.x;
-    if (r >= n_rooms) return;
+__device__ __forceinline__ void room_beta_kernel_body(RoomDesc *rooms, int r, const float *beta) {
     RoomDesc &R = rooms[r];
     const int w = threadIdx.x;   // one thread per wall
     if (w < 6) {
@@ -34,6 +32,42 @@ __global__ void room_beta_kernel(RoomDesc *rooms, int n_rooms, const float *beta
                          ((1.0f - b[4] * b[4]) + (1.0f - b[5] * b[5])) * R.L[0] * R.L[1];
         R.T60 = 0.161f * (R.L[0] * R.L[1] * R.L[2]) / Sa;
     }
+}
+
+__global__ void room_beta_kernel(RoomDesc *rooms, int n_rooms, const float *beta) {
+    if ((int)blockIdx.x < n_rooms) room_beta_kernel_body(rooms, blockIdx.x, beta);
+}
+
+// room_beta_kernel's work in blocks [0, n_rooms) and, in the blocks after them, the
+// per-item skip flags of item_skip_kernel (independent of beta: room geometry and
+// positions only), so that a differentiable forward step needs one launch for both.
+__global__ void room_beta_skip_kernel(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
+                                      int n_items, const float *pos_src, const float *pos_rcv,
+                                      unsigned char *skip) {
+    if ((int)blockIdx.x < n_rooms) {
+        if (threadIdx.x < 32) room_beta_kernel_body(rooms, blockIdx.x, beta);
+        return;
+    }
+    const int k = (blockIdx.x - n_rooms) * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    const IsmItem it = items[k];
+    unsigned char m = 0;
+    if (it.t_lo > 0) {
+        const RoomDesc &R = rooms[it.room];
+        const float s3[3] = {pos_src[3 * it.src], pos_src[3 * it.src + 1], pos_src[3 * it.src + 2]};
+        const float r3[3] = {pos_rcv[3 * it.rcv], pos_rcv[3 * it.rcv + 1], pos_rcv[3 * it.rcv + 2]};
+        m = images_miss_segment(R.L, R.nb, s3, r3, R.kh, R.H, it.t_lo, it.t_hi) ? 1 : 0;
+    }
+    skip[k] = m;
+}
+
+cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
+                                  int n_items, const float *pos_src, const float *pos_rcv, unsigned char *skip,
+                                  cudaStream_t st) {
+    const int blocks = n_rooms + (n_items + 255) / 256;
+    if (blocks <= 0) return cudaSuccess;
+    room_beta_skip_kernel<<<blocks, 256, 0, st>>>(rooms, n_rooms, beta, items, n_items, pos_src, pos_rcv, skip);
+    return cudaGetLastError();
 }
 
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st) {
