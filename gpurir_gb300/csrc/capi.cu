@@ -86,6 +86,9 @@ static const size_t kSmemBudget = 113 * 1024;   // two blocks per SM (228 KB les
 static const size_t kSmemBudgetLarge = 220 * 1024;
 static const long kPartImages = 2048;   // fewest images per part of a split RIR (one chunk)
 
+struct PlanCache;
+static void free_plan_cache(PlanCache *c);
+
 struct gpurir_sim {
     int mp = 0, lut = 0;
     uint64_t seed = 1234, calls = 0;
@@ -117,6 +120,12 @@ struct gpurir_sim {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_ism = false, ev_tail = false;
     int last_launches = 0;        // kernels the last simulate call launched
+    // The plan of the last simulate call, reused by a call with the same room shapes
+    // (sizes, image counts, lengths, source/receiver counts: what the work items depend
+    // on); its items stay on the device while ws_gen == the generation they were
+    // staged under (a reallocation or another call's upload bumps ws_gen).
+    PlanCache *pcache = nullptr;
+    uint64_t ws_gen = 0;
     uint64_t last_h2d = 0, last_d2h = 0;
     // convolution: twiddle tables per FFT size, and a grow-only workspace
     std::vector<std::pair<int, float2 *>> twiddles;
@@ -171,6 +180,7 @@ extern "C" int gpurir_destroy(gpurir_sim *s) {
     if (!s) return GPURIR_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->d_ws) cudaFree(s->d_ws);
+    free_plan_cache(s->pcache);
     s->stage_ring[s->stage_slot].h = s->h_stage;
     for (int k = 0; k < gpurir_sim::kStageRing; k++)
         if (s->stage_ring[k].h) cudaFreeHost(s->stage_ring[k].h);
@@ -328,6 +338,7 @@ static int ensure_device(gpurir_sim *s, size_t bytes) {
     s->d_ws = nullptr;
     s->d_ws_bytes = 0;
     size_t want = align_up(bytes + bytes / 4, 1 << 20);
+    s->ws_gen++;
     CK(cudaMalloc(&s->d_ws, want));
     s->d_ws_bytes = want;
     return GPURIR_OK;
@@ -544,13 +555,14 @@ struct Layout {
 static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv, long M,
                           long long out_elems, bool host_io) {
     Layout L;
+    // rooms and positions first: the part of an upload that changes from call to call
     L.o_rooms = 0;
-    L.o_items = align_up(L.o_rooms + n_rooms * sizeof(RoomDesc), 256);
+    L.o_pos = align_up(L.o_rooms + n_rooms * sizeof(RoomDesc), 256);
+    size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
+    L.o_items = align_up(L.o_pos + n_pos * sizeof(float), 256);
     L.o_rirs = align_up(L.o_items + P.items.size() * sizeof(IsmItem), 256);
     L.o_groups = align_up(L.o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
-    L.o_pos = align_up(L.o_groups + P.groups.size() * sizeof(PartGroup), 256);
-    size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
-    L.stage_bytes = align_up(L.o_pos + n_pos * sizeof(float), 256);
+    L.stage_bytes = align_up(L.o_groups + P.groups.size() * sizeof(PartGroup), 256);
     L.o_env = L.stage_bytes;
     L.o_axis = align_up(L.o_env + (size_t)M * 3 * sizeof(float), 256);
     L.o_part = align_up(L.o_axis + (size_t)P.grid * P.axis_cap * sizeof(float4), 256);
@@ -558,6 +570,42 @@ static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv,
     L.o_out = align_up(L.o_skip + (P.skip_flags ? P.items.size() : 0), 256);
     L.dev_bytes = L.o_out + (host_io ? (size_t)out_elems * sizeof(float) : 0);
     return L;
+}
+
+struct PlanCache {
+    std::vector<double> key;
+    Plan P;
+    Layout L;
+    uint64_t gen = ~0ull;   // ws_gen under which P's items were uploaded
+};
+
+static void free_plan_cache(PlanCache *c) { delete c; }
+
+// What the plan of simulate_rooms depends on: per room the sizes, image counts,
+// lengths, window, Fs/c, source/receiver counts and patterns; the evaluation mode;
+// where the output goes.
+static std::vector<double> plan_key(const gpurir_sim *s, const std::vector<RoomDesc> &R, bool host_io,
+                                    long long out_elems) {
+    std::vector<double> k;
+    k.reserve(4 + 16 * R.size());
+    k.push_back((double)s->mp);
+    k.push_back((double)s->lut);
+    k.push_back(host_io ? 1.0 : 0.0);
+    k.push_back((double)out_elems);
+    for (const RoomDesc &r : R) {
+        for (int a = 0; a < 3; a++) k.push_back(r.L[a]);
+        for (int a = 0; a < 3; a++) k.push_back((double)r.nb[a]);
+        k.push_back((double)r.n_ism);
+        k.push_back((double)r.n_total);
+        k.push_back((double)r.n_src);
+        k.push_back((double)r.n_rcv);
+        k.push_back(r.H);
+        k.push_back(r.kh);
+        k.push_back(r.kl);
+        k.push_back((double)r.spkr);
+        k.push_back((double)r.mic);
+    }
+    return k;
 }
 
 static void fill_stage(char *h, const Layout &L, const std::vector<RoomDesc> &R, const Plan &P) {
@@ -647,15 +695,29 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
                           const float *pos_src, const float *pos_rcv, const float *orV_src,
                           const float *orV_rcv, float *out, long long out_elems, bool host_io,
                           cudaStream_t st, const float *d_beta = nullptr) {
-    Plan P;
-    int rc = plan_rooms(s, R, P);
-    if (rc) return rc;
+    int rc;
+    std::vector<double> key = plan_key(s, R, host_io, out_elems);
+    const bool hit = s->pcache && s->pcache->key == key;
+    if (!hit) {
+        if (!s->pcache) s->pcache = new PlanCache();
+        s->pcache->key.clear();   // invalid until planned
+        s->pcache->gen = ~0ull;
+        if ((rc = plan_rooms(s, R, s->pcache->P))) return rc;
+        s->pcache->key = std::move(key);
+    }
+    const Plan &P = s->pcache->P;
     const long M = (long)P.rirs.size();
-    Layout L = make_layout(P, R.size(), n_src, n_rcv, M, out_elems, host_io);
+    if (!hit) s->pcache->L = make_layout(P, R.size(), n_src, n_rcv, M, out_elems, host_io);
+    const Layout &L = s->pcache->L;
     if ((rc = ensure_device(s, L.dev_bytes))) return rc;
     if ((rc = ensure_stage(s, L.stage_bytes))) return rc;
+    // the items of an unchanged plan are still on the device unless something else
+    // was uploaded there since: then only the rooms and positions go up
+    const bool items_resident = hit && s->pcache->gen == s->ws_gen;
+    const size_t up_bytes = items_resident ? L.o_items : L.stage_bytes;
     char *h = s->h_stage;
-    fill_stage(h, L, R, P);
+    if (items_resident) memcpy(h + L.o_rooms, R.data(), R.size() * sizeof(RoomDesc));
+    else fill_stage(h, L, R, P);
     const float *dps = pos_src, *dpr = pos_rcv, *dos = orV_src, *dor = orV_rcv;
     char *d = s->d_ws;
     if (host_io) {
@@ -670,9 +732,10 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
         dps = dp; dpr = dp + 3 * n_src; dos = dp + 3 * (n_src + n_rcv); dor = dp + 3 * (2 * n_src + n_rcv);
     }
     if (s->ws_recorded) CK(cudaStreamWaitEvent(st, s->ws_busy, 0));   // earlier calls, any stream
-    CK(cudaMemcpyAsync(d, h, L.stage_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d, h, up_bytes, cudaMemcpyHostToDevice, st));
     CK(cudaEventRecord(s->stage_done, st));
     s->stage_pending = true;
+    if (!items_resident) s->pcache->gen = ++s->ws_gen;
     if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(d + L.o_rooms), (int)R.size(), d_beta, st));
     float *dout = host_io ? reinterpret_cast<float *>(d + L.o_out) : out;
     // Host output the GPU can store to directly (pinned memory, or any host memory on
@@ -685,7 +748,7 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     }
     s->last_direct = direct;
     s->ev_ism = s->ev_tail = false;
-    s->last_h2d = L.stage_bytes;
+    s->last_h2d = up_bytes;
     s->last_d2h = sizeof(int) + (host_io ? (uint64_t)out_elems * sizeof(float) : 0);
     if ((rc = enqueue_kernels(s, P, d, L, M, dps, dpr, dos, dor, dout, s->d_ctl, nullptr, st, true)))
         return rc;
@@ -1103,6 +1166,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     char *d = s->d_ws;
     if (s->ws_recorded) CK(cudaStreamWaitEvent(st, s->ws_busy, 0));
     CK(cudaMemcpyAsync(d, h, stage_bytes, cudaMemcpyHostToDevice, st));
+    s->ws_gen++;   // the cached plan's items were overwritten
     CK(cudaEventRecord(s->stage_done, st));
     s->stage_pending = true;
     if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(d + o_rooms), n_rooms, d_beta, st));

@@ -285,3 +285,77 @@ def test_segments_past_the_last_image(built):
     assert np.abs(ref[1, :, late]).max() > 1e-4 * np.abs(ref).max()
     assert np.abs(out[1, :, late] - ref[1, :, late]).max() <= 1e-5 * np.abs(ref).max()
     assert not np.any(out[:, :, 1000:n])
+
+
+def _one_shot_adjoint(sim, rooms, g, fs=16000.0):
+    """gpurir_ism_backward_batch_device on torch tensors: gradients of sum(h * g)."""
+    import ctypes
+    import torch
+    from gpurir_gb300 import _lib
+    from gpurir_gb300.batch import _room_struct
+    dev = torch.device("cuda")
+    ps = torch.tensor(np.concatenate([r["pos_src"] for r in rooms]), device=dev)
+    pr = torch.tensor(np.concatenate([r["pos_rcv"] for r in rooms]), device=dev)
+    gr = torch.tensor(g, dtype=torch.float32, device=dev)
+    gb = torch.empty((len(rooms), 6), device=dev)
+    gs, gq = torch.empty_like(ps), torch.empty_like(pr)
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.load().gpurir_ism_backward_batch_device(
+        sim.handle, len(rooms), _room_struct(rooms), fs, 343.0, ps.data_ptr(), pr.data_ptr(), None, None,
+        gr.data_ptr(), gb.data_ptr(), gs.data_ptr(), gq.data_ptr(), None, None, ctypes.c_void_p(st)),
+        "gpurir_ism_backward_batch_device")
+    torch.cuda.synchronize()
+    return gb.cpu().numpy(), gs.cpu().numpy(), gq.cpu().numpy()
+
+
+def test_plan_reuse_across_calls_and_other_uploads(built):
+    """Calls with the same room shapes reuse the plan and the work items already on the
+    device; new positions and walls must still take effect, and an upload by another
+    entry (the one-shot adjoint) in between must not leave stale items behind."""
+    rng = np.random.default_rng(21)
+    room, nb, T = [5.0, 4.0, 3.0], [7, 8, 9], 0.12
+    sim = _sim()
+
+    def check(ps, pr, beta, nb_=nb, label=""):
+        out, ref, parts = _run(sim, room, beta, ps, pr, nb_, T, 16000.0)
+        _check_ism(out, ref, parts["n_ism"], label)
+        return out
+
+    shapes = lambda: (_rand_inside(rng, 3, room, 0.5), _rand_inside(rng, 5, room, 0.5),
+                      rng.uniform(0.5, 0.95, 6).astype(np.float32))
+    a = check(*shapes(), label="first call")
+    b = check(*shapes(), label="same shapes, new positions and walls")
+    assert not np.array_equal(a, b)
+    ps, pr, beta = shapes()
+    n = oracle.n_samples(T, 16000.0)
+    _one_shot_adjoint(sim, [dict(room_sz=np.float32(room), beta=beta, pos_src=ps, pos_rcv=pr, nb_img=[5, 5, 5],
+                                 Tmax=0.05, Tdiff=0.05)],
+                      rng.standard_normal(3 * 5 * oracle.n_samples(0.05, 16000.0)))
+    check(*shapes(), label="after another entry's upload")
+    check(*shapes(), nb_=[6, 6, 6], label="new shapes")
+    check(*shapes(), label="back to the first shapes")
+    assert n > 0
+
+
+def test_one_shot_adjoint_matches_torch_batch(built):
+    """gpurir_ism_backward_batch_device gives the gradients of the prepared-batch path."""
+    import torch
+    from gpurir_gb300.autograd import TorchBatch
+    rng = np.random.default_rng(23)
+    rooms = []
+    for i in range(3):
+        room = rng.uniform([3, 3, 2.5], [6, 5, 3.5]).astype(np.float32)
+        rooms.append(dict(room_sz=room, beta=rng.uniform(0.6, 0.9, 6).astype(np.float32),
+                          pos_src=_rand_inside(rng, 2, room, 0.5), pos_rcv=_rand_inside(rng, 3, room, 0.5),
+                          nb_img=[5, 6, 7], Tmax=0.05 + 0.01 * i, Tdiff=0.05 + 0.01 * i))
+    sim = _sim()
+    model = TorchBatch(rooms, 16000.0, sim=sim)
+    g = rng.standard_normal(model.total)
+    t = lambda a: torch.tensor(a, device="cuda", requires_grad=True)
+    beta = t(np.stack([r["beta"] for r in rooms]))
+    ps, pr = t(np.concatenate([r["pos_src"] for r in rooms])), t(np.concatenate([r["pos_rcv"] for r in rooms]))
+    (model(beta, ps, pr) * torch.tensor(g, dtype=torch.float32, device="cuda")).sum().backward()
+    gb, gs, gq = _one_shot_adjoint(sim, rooms, g)
+    for ours, ref in ((gb, beta.grad), (gs, ps.grad), (gq, pr.grad)):
+        ref = ref.cpu().numpy()
+        assert rel_l2(ours, ref) < 1e-6, rel_l2(ours, ref)
