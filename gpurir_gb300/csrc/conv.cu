@@ -229,6 +229,9 @@ constexpr float kR2 = 0.70710678118654752f;    // sqrt(2)/2
 
 __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 
+// rows transformed together per block by rir_conv_reg_kernel
+constexpr int kConvRows = 2;
+
 // x * (-i) (forward) or x * (+i) (inverse)
 template <bool INV>
 __device__ __forceinline__ float2 rot_q(float2 a) {
@@ -370,6 +373,96 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[16], float2 *buf, const floa
     __syncthreads();
 }
 
+// ROWS transforms at once (rows q at buf + q * pad16(M)): the same passes, barriers
+// and twiddle loads serve every row, and each thread has ROWS independent DFTs in
+// flight per pass.
+template <bool INV, int M, int ROWS>
+__device__ __forceinline__ void pass16_rows(float2 (&v)[ROWS][16], float2 *buf, int j, int Ns,
+                                            const float2 *__restrict__ W) {
+    constexpr int BS = M + M / 16;
+    const int k = j & (Ns - 1);
+    if (Ns > 1) {
+        const int step = (2 * M) / (Ns * 16);
+#pragma unroll
+        for (int r = 1; r < 16; r++) {
+            float2 w = __ldg(&W[r * k * step]);
+            if (INV) w = cconj(w);
+#pragma unroll
+            for (int q = 0; q < ROWS; q++) v[q][r] = cmul(v[q][r], w);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < ROWS; q++) dft16<INV>(v[q]);
+    const int base = (j - k) * 16 + k;
+#pragma unroll
+    for (int q = 0; q < ROWS; q++)
+#pragma unroll
+        for (int s = 0; s < 16; s++) buf[q * BS + pad16(base + s * Ns)] = v[q][dr16(s)];
+}
+
+template <bool INV, int M, bool LOADED, int ROWS>
+__device__ __forceinline__ void reg_fft_rows(float2 (&v)[ROWS][16], float2 *buf, const float2 *__restrict__ W) {
+    constexpr int T = M / 16, BS = M + M / 16;
+    const int j = threadIdx.x;
+    if (!LOADED) {
+#pragma unroll
+        for (int q = 0; q < ROWS; q++)
+#pragma unroll
+            for (int r = 0; r < 16; r++) v[q][r] = buf[q * BS + pad16(j + r * T)];
+        __syncthreads();
+    }
+    pass16_rows<INV, M, ROWS>(v, buf, j, 1, W);
+    __syncthreads();
+    int Ns = 16;
+#pragma unroll 1
+    for (; Ns * 16 <= M; Ns *= 16) {
+#pragma unroll
+        for (int q = 0; q < ROWS; q++)
+#pragma unroll
+            for (int r = 0; r < 16; r++) v[q][r] = buf[q * BS + pad16(j + r * T)];
+        __syncthreads();
+        pass16_rows<INV, M, ROWS>(v, buf, j, Ns, W);
+        __syncthreads();
+    }
+    if (Ns < M) {   // last pass, radix R = M / Ns in {2, 4, 8}, as in reg_fft
+        const int R = M / Ns;
+        for (int g = 0; g < 16 / R; g++) {
+            const int jj = j + T * g;
+            float2 a[ROWS][8];
+#pragma unroll
+            for (int q = 0; q < ROWS; q++)
+                for (int r = 0; r < R; r++) a[q][r] = buf[q * BS + pad16(jj + r * Ns)];
+            for (int r = 1; r < R; r++) {
+                float2 w = __ldg(&W[r * jj * 2]);   // W_M^1 = W_N^2
+                if (INV) w = cconj(w);
+#pragma unroll
+                for (int q = 0; q < ROWS; q++) a[q][r] = cmul(a[q][r], w);
+            }
+#pragma unroll
+            for (int q = 0; q < ROWS; q++) {
+                if (R == 2) {
+                    dft2<INV>(a[q][0], a[q][1]);
+                } else if (R == 4) {
+                    dft4<INV>(a[q][0], a[q][1], a[q][2], a[q][3]);
+                } else {
+                    dft4<INV>(a[q][0], a[q][2], a[q][4], a[q][6]);
+                    dft4<INV>(a[q][1], a[q][3], a[q][5], a[q][7]);
+                    const float2 w1 = make_float2(kR2, INV ? kR2 : -kR2);
+                    const float2 w3 = make_float2(-kR2, INV ? kR2 : -kR2);
+                    const float2 o1 = cmul(a[q][3], w1), o2 = rot_q<INV>(a[q][5]), o3 = cmul(a[q][7], w3);
+                    const float2 e0 = a[q][0], e1 = a[q][2], e2 = a[q][4], e3 = a[q][6], o0 = a[q][1];
+                    a[q][0] = cadd(e0, o0); a[q][4] = csub(e0, o0);
+                    a[q][1] = cadd(e1, o1); a[q][5] = csub(e1, o1);
+                    a[q][2] = cadd(e2, o2); a[q][6] = csub(e2, o2);
+                    a[q][3] = cadd(e3, o3); a[q][7] = csub(e3, o3);
+                }
+                for (int s = 0; s < R; s++) buf[q * BS + pad16(jj + s * Ns)] = a[q][s];
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // Pass-1 inputs of thread j straight from global memory: z[n] = x[2n] + i x[2n+1],
 // n = j + r M/16, zero past `len` (8-byte loads when the row allows).
 template <int M>
@@ -423,65 +516,80 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) segment_spectra_reg_kernel(
     }
 }
 
-template <int M>
-__global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
+template <int M, int ROWS>
+__global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / ROWS : 1)) rir_conv_reg_kernel(
         const float *__restrict__ rir, int P, int R, int L, int S, const float2 *__restrict__ W,
         const float2 *__restrict__ Sg, float *__restrict__ out, long out_ld) {
-    constexpr int T = M / 16;
+    constexpr int T = M / 16, BS = M + M / 16;
     extern __shared__ __align__(16) float2 sm[];
-    float2 *buf = sm;   // pad16(M) elements
+    float2 *buf = sm;   // ROWS buffers of pad16(M) elements
     const int j = threadIdx.x;
     const int n_out = S + L - 1;
-    float2 v[16];
+    float2 v[ROWS][16];
     const bool vec_out = (out_ld & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-    for (int pr = blockIdx.x; pr < P * R; pr += gridDim.x) {
-        const int p = pr / R;
-        const float *x = rir + (size_t)pr * L;
-        if (j == 0 && pr + (int)gridDim.x < P * R) {
-            // the block's next RIR row into L2 while this row is transformed (whole
-            // 16-byte units inside the row only)
-            const uintptr_t a = reinterpret_cast<uintptr_t>(rir + (size_t)(pr + gridDim.x) * L);
-            const uintptr_t lo = (a + 15) & ~(uintptr_t)15, hi = (a + (size_t)L * sizeof(float)) & ~(uintptr_t)15;
+    const int n_rows = P * R;
+    for (int pr0 = blockIdx.x * ROWS; pr0 < n_rows; pr0 += gridDim.x * ROWS) {
+        const int nq = min(ROWS, n_rows - pr0);   // rows of this group (uniform over the block)
+        if (j == 0 && pr0 + (int)gridDim.x * ROWS < n_rows) {
+            // the block's next RIR rows into L2 while these are transformed (whole 16-byte
+            // units inside the rows only)
+            const int nn = min(ROWS, n_rows - (pr0 + (int)gridDim.x * ROWS));
+            const uintptr_t a = reinterpret_cast<uintptr_t>(rir + (size_t)(pr0 + gridDim.x * ROWS) * L);
+            const uintptr_t lo = (a + 15) & ~(uintptr_t)15, hi = (a + (size_t)nn * L * sizeof(float)) & ~(uintptr_t)15;
             if (hi > lo)
                 asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo))
                              : "memory");
         }
-        load_packed<M>(x, L, v);
-        reg_fft<false, M, true>(v, buf, W);
+#pragma unroll
+        for (int q = 0; q < ROWS; q++) {
+            if (q < nq) {
+                load_packed<M>(rir + (size_t)(pr0 + q) * L, L, v[q]);
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; r++) v[q][r] = make_float2(0.0f, 0.0f);
+            }
+        }
+        reg_fft_rows<false, M, true, ROWS>(v, buf, W);
         // spectrum of the RIR at k and M - k, times the segment's spectrum, repacked
         // for the inverse real FFT (same algebra as rir_conv_kernel)
-        const float2 *sp = Sg + (size_t)p * (M + 1);
-        for (int k = j; k <= M / 2; k += T) {
-            const int km = (M - k) & (M - 1);
-            const float2 zk = buf[pad16(k)], zm = buf[pad16(km)];
-            const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-            const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-            const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
-            const float2 wk = __ldg(&W[k]);
-            const float2 wm = make_float2(-wk.x, wk.y);
-            const float2 yk = cmul(cadd(ze, cmul(wk, zo)), __ldg(&sp[k]));
-            const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), __ldg(&sp[M - k]));
-            const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
-            const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
-            buf[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
-            if (k != 0 && km != k) {
-                const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
-                const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
-                buf[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+        for (int q = 0; q < nq; q++) {
+            float2 *bq = buf + q * BS;
+            const float2 *sp = Sg + (size_t)((pr0 + q) / R) * (M + 1);
+            for (int k = j; k <= M / 2; k += T) {
+                const int km = (M - k) & (M - 1);
+                const float2 zk = bq[pad16(k)], zm = bq[pad16(km)];
+                const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+                const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+                const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+                const float2 wk = __ldg(&W[k]);
+                const float2 wm = make_float2(-wk.x, wk.y);
+                const float2 yk = cmul(cadd(ze, cmul(wk, zo)), __ldg(&sp[k]));
+                const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), __ldg(&sp[M - k]));
+                const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
+                const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
+                bq[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
+                if (k != 0 && km != k) {
+                    const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
+                    const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
+                    bq[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+                }
             }
         }
         __syncthreads();
-        reg_fft<true, M, false>(v, buf, W);
-        float *o = out + (size_t)pr * out_ld;
-        if (vec_out) {   // rows padded to whole float4: the 0..3 floats past n_out land in the padding
-            for (int q = j; 4 * q < n_out; q += T) {
-                const float2 z0 = buf[pad16(2 * q)], z1 = buf[pad16(2 * q + 1)];
-                reinterpret_cast<float4 *>(o)[q] = make_float4(z0.x, z0.y, z1.x, z1.y);
-            }
-        } else {
-            for (int i = j; i < n_out; i += T) {
-                const float2 z = buf[pad16(i >> 1)];
-                o[i] = (i & 1) ? z.y : z.x;
+        reg_fft_rows<true, M, false, ROWS>(v, buf, W);
+        for (int q = 0; q < nq; q++) {
+            const float2 *bq = buf + q * BS;
+            float *o = out + (size_t)(pr0 + q) * out_ld;
+            if (vec_out) {   // rows padded to whole float4: the 0..3 floats past n_out land in the padding
+                for (int c = j; 4 * c < n_out; c += T) {
+                    const float2 z0 = bq[pad16(2 * c)], z1 = bq[pad16(2 * c + 1)];
+                    reinterpret_cast<float4 *>(o)[c] = make_float4(z0.x, z0.y, z1.x, z1.y);
+                }
+            } else {
+                for (int i = j; i < n_out; i += T) {
+                    const float2 z = bq[pad16(i >> 1)];
+                    o[i] = (i & 1) ? z.y : z.x;
+                }
             }
         }
         __syncthreads();
@@ -491,21 +599,22 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) rir_conv_reg_kernel(
 template <int M>
 static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S, const float2 *W,
                                    const float2 *Sg, float *out, long out_ld, cudaStream_t st) {
-    const size_t smem = (size_t)(M + M / 16) * sizeof(float2);
+    constexpr int ROWS = kConvRows;
+    const size_t smem = (size_t)ROWS * (M + M / 16) * sizeof(float2);
     static int blocks = -1;
     if (blocks < 0) {
-        cudaError_t e = cudaFuncSetAttribute(rir_conv_reg_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(rir_conv_reg_kernel<M, ROWS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         int per_sm = 0, dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rir_conv_reg_kernel<M>, M / 16, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rir_conv_reg_kernel<M, ROWS>, M / 16, smem);
         if (e != cudaSuccess) return e;
         blocks = std::max(1, per_sm) * std::max(1, sms);
     }
-    const int grid = std::min(P * R, blocks);
-    rir_conv_reg_kernel<M><<<grid, M / 16, smem, st>>>(rir, P, R, L, S, W, Sg, out, out_ld);
+    const int grid = std::min((P * R + ROWS - 1) / ROWS, blocks);
+    rir_conv_reg_kernel<M, ROWS><<<grid, M / 16, smem, st>>>(rir, P, R, L, S, W, Sg, out, out_ld);
     return cudaGetLastError();
 }
 
