@@ -25,7 +25,8 @@ def segment_signal(source_signal, n_pts, timestamps=None, fs=None):
     width = int(w_len.max())
     sig = np.asarray(source_signal)
     if np.all(w_len == width) and np.array_equal(w_ini[:-1], width * np.arange(n_pts)):
-        segments = sig[:n_pts * width].reshape(n_pts, width).astype(np.float32)   # back to back
+        # back to back: a view of a float32 signal, no copy
+        segments = sig[:n_pts * width].reshape(n_pts, width).astype(np.float32, copy=False)
     else:
         segments = np.zeros((n_pts, width), dtype=np.float32)
         for p in range(n_pts):
