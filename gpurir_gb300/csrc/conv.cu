@@ -289,6 +289,27 @@ __device__ __forceinline__ void dft16(float2 (&v)[16]) {
 
 __host__ __device__ constexpr int dr16(int s) { return 4 * (s & 3) + (s >> 2); }
 
+// Twiddles w^r, r = 1..15, of one radix-16 pass (w = W[e]): w, w^2, w^4, w^8 from the
+// table, the others as products of at most three of them (4 loads instead of 15; error
+// within 3 roundings).
+__device__ __forceinline__ void twiddle_powers(const float2 *__restrict__ W, int e, float2 (&t)[16]) {
+    t[1] = __ldg(&W[e]);
+    t[2] = __ldg(&W[2 * e]);
+    t[4] = __ldg(&W[4 * e]);
+    t[8] = __ldg(&W[8 * e]);
+    t[3] = cmul(t[1], t[2]);
+    t[5] = cmul(t[1], t[4]);
+    t[6] = cmul(t[2], t[4]);
+    t[7] = cmul(t[3], t[4]);
+    t[9] = cmul(t[1], t[8]);
+    t[10] = cmul(t[2], t[8]);
+    t[11] = cmul(t[3], t[8]);
+    t[12] = cmul(t[4], t[8]);
+    t[13] = cmul(t[5], t[8]);
+    t[14] = cmul(t[6], t[8]);
+    t[15] = cmul(t[7], t[8]);
+}
+
 // One radix-16 Stockham pass at stride Ns for the thread's j (= thread index):
 // twiddle, DFT, write dst[(j - k) 16 + k + s Ns], k = j mod Ns.
 // W: exp(-2 pi i m/N) for m < N = 2M.
@@ -297,13 +318,10 @@ __device__ __forceinline__ void pass16_compute_write(float2 (&v)[16], float2 *bu
                                                      const float2 *__restrict__ W) {
     const int k = j & (Ns - 1);
     if (Ns > 1) {
-        const int step = (2 * M) / (Ns * 16);   // W_{16 Ns}^1 = W_N^step
+        float2 t[16];
+        twiddle_powers(W, k * ((2 * M) / (Ns * 16)), t);   // W_{16 Ns}^1 = W_N^step
 #pragma unroll
-        for (int r = 1; r < 16; r++) {
-            float2 w = __ldg(&W[r * k * step]);
-            if (INV) w = cconj(w);
-            v[r] = cmul(v[r], w);
-        }
+        for (int r = 1; r < 16; r++) v[r] = cmul(v[r], INV ? cconj(t[r]) : t[r]);
     }
     dft16<INV>(v);
     const int base = (j - k) * 16 + k;
@@ -382,11 +400,11 @@ __device__ __forceinline__ void pass16_rows(float2 (&v)[ROWS][16], float2 *buf, 
     constexpr int BS = M + M / 16;
     const int k = j & (Ns - 1);
     if (Ns > 1) {
-        const int step = (2 * M) / (Ns * 16);
+        float2 t[16];
+        twiddle_powers(W, k * ((2 * M) / (Ns * 16)), t);
 #pragma unroll
         for (int r = 1; r < 16; r++) {
-            float2 w = __ldg(&W[r * k * step]);
-            if (INV) w = cconj(w);
+            const float2 w = INV ? cconj(t[r]) : t[r];
 #pragma unroll
             for (int q = 0; q < ROWS; q++) v[q][r] = cmul(v[q][r], w);
         }
