@@ -569,27 +569,44 @@ __global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / RO
         }
         reg_fft_rows<false, M, true, ROWS>(v, buf, W);
         // spectrum of the RIR at k and M - k, times the segment's spectrum, repacked
-        // for the inverse real FFT (same algebra as rir_conv_kernel)
+        // for the inverse real FFT (same algebra as rir_conv_kernel).  The thread's k are
+        // j + i T; their twiddles and segment spectra are loaded four k at a time before
+        // any arithmetic (the transform's registers are free here), not one round trip
+        // per k.
         for (int q = 0; q < nq; q++) {
             float2 *bq = buf + q * BS;
             const float2 *sp = Sg + (size_t)((pr0 + q) / R) * (M + 1);
-            for (int k = j; k <= M / 2; k += T) {
-                const int km = (M - k) & (M - 1);
-                const float2 zk = bq[pad16(k)], zm = bq[pad16(km)];
-                const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-                const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-                const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
-                const float2 wk = __ldg(&W[k]);
-                const float2 wm = make_float2(-wk.x, wk.y);
-                const float2 yk = cmul(cadd(ze, cmul(wk, zo)), __ldg(&sp[k]));
-                const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), __ldg(&sp[M - k]));
-                const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
-                const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
-                bq[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
-                if (k != 0 && km != k) {
-                    const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
-                    const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
-                    bq[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+            for (int k0 = j; k0 <= M / 2; k0 += 4 * T) {
+                float2 wk4[4], sk4[4], sm4[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int k = k0 + i * T;
+                    const int kk = min(k, M / 2);   // in bounds; results of k > M / 2 unused
+                    wk4[i] = __ldg(&W[kk]);
+                    sk4[i] = __ldg(&sp[kk]);
+                    sm4[i] = __ldg(&sp[M - kk]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int k = k0 + i * T;
+                    if (k > M / 2) break;
+                    const int km = (M - k) & (M - 1);
+                    const float2 zk = bq[pad16(k)], zm = bq[pad16(km)];
+                    const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+                    const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+                    const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+                    const float2 wk = wk4[i];
+                    const float2 wm = make_float2(-wk.x, wk.y);
+                    const float2 yk = cmul(cadd(ze, cmul(wk, zo)), sk4[i]);
+                    const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), sm4[i]);
+                    const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
+                    const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
+                    bq[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
+                    if (k != 0 && km != k) {
+                        const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
+                        const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
+                        bq[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+                    }
                 }
             }
         }
