@@ -228,14 +228,33 @@ def _extra_batched(G, B, workloads, sim, flush, stream, fs, dev):
     plain()
     t_plain = _timed(plain, 3, stream, flush)
     upd = sum(workloads.windowed_updates_torch(dict(r, fs=fs)) for r in rooms)
+    # the plain single-room configuration (2 RIRs, 0.5 s, full ISM) through the same entry
+    pr_scene = workloads.plain_room()
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
+    p_ps, p_pr = d(pr_scene["pos_src"]), d(pr_scene["pos_rcv"])
+    p_out = torch.empty((p_ps.shape[0], p_pr.shape[0], workloads.n_samples(pr_scene["Tmax"], fs)), device=dev)
+
+    def single():
+        sim.simulate_rir_device(pr_scene["room_sz"], pr_scene["beta"], p_ps, p_pr, None, None, 0, 0,
+                                pr_scene["nb_img"], pr_scene["Tdiff"], pr_scene["Tmax"], fs, 343.0, p_out,
+                                stream.cuda_stream)
+
+    single()
+    t_single = _timed(single, 20, stream, flush)
+    n_single = p_ps.shape[0] * p_pr.shape[0]
+    upd_single = workloads.windowed_updates_torch(dict(pr_scene, fs=fs))
     out["batched_rooms"] = {
         "rooms": len(rooms), "rirs": n_rir, "windowed_updates": upd,
         "batched_ms": t_batch, "batched_rirs_per_s": n_rir / (t_batch * 1e-3),
         "batched_updates_per_s": upd / (t_batch * 1e-3),
         "plain_loop_ms": t_plain, "plain_loop_rirs_per_s": n_rir / (t_plain * 1e-3),
         "batched_over_plain": t_plain / t_batch,
+        "plain_room_ms": t_single, "plain_room_rirs_per_s": n_single / (t_single * 1e-3),
+        "plain_room_updates_per_s": upd_single / (t_single * 1e-3),
+        "batched_over_plain_room_updates": (upd / t_batch) / (upd_single / t_single),
         "note": "batched = one CUDA-graph replay of all 512 rooms; plain = one device-API call "
-                "per room on the same stream"}
+                "per room on the same stream; plain_room = the plain single-room configuration "
+                "(2 RIRs, 0.5 s, full ISM) per device-API call"}
     return out
 
 
