@@ -40,12 +40,12 @@ cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, i
 cudaError_t philox_stream_launch(uint32_t *out, long n, uint64_t seed, uint64_t offset,
                                  uint32_t rir, cudaStream_t st);
 cudaError_t probe_peaks(double *fp32_flops, double *mufu_ops, cudaStream_t st);
-size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad);
+size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad, int axis_cap);
 cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                 const float *pos_src, const float *pos_rcv, const float *orv_src,
                                 const float *orv_rcv, const float *grad, float *item_grad,
-                                int *work_counter, int *status, int max_tseg, int grid, int clamp,
-                                cudaStream_t st);
+                                int *work_counter, int *status, int max_tseg, int axis_cap, int grid,
+                                int clamp, cudaStream_t st);
 cudaError_t grad_reduce_launch(const float *item_grad, const int *const csr[6], int n_rooms, int n_src,
                                int n_rcv, float *const out[5], cudaStream_t st);
 int ism_backward_blocks_per_sm(int tpl, int clamp, size_t smem);
@@ -1133,7 +1133,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
     int max_tseg = 1;
     for (const IsmItem &it : P.items) max_tseg = std::max(max_tseg, it.t_hi - it.t_lo);
     const int pad = 64 * P.tpl;
-    const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad);
+    const size_t smem = ism_backward_smem_bytes(P.tpl, max_tseg, pad, P.axis_cap);
     int bps = 0;
     if (!P.items.empty()) {
         if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
@@ -1178,7 +1178,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
         CK(ism_backward_launch(P.tpl, reinterpret_cast<const RoomDesc *>(d + o_rooms),
                                reinterpret_cast<const IsmItem *>(d + o_items), n_items, d_pos_src,
                                d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, s->d_ctl, s->d_ctl + 1,
-                               max_tseg, grid, P.clamp, st));
+                               max_tseg, P.axis_cap, grid, P.clamp, st));
     }
     const int *dp[6];
     for (int a = 0; a < 6; a++) dp[a] = reinterpret_cast<const int *>(d + o_arr[a]);
@@ -1234,13 +1234,14 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
     a->M = (long)P.rirs.size();
     a->L = make_layout(P, R.size(), a->ns, a->nr, a->M, a->out_elems, false);
     for (const IsmItem &it : P.items) a->max_tseg = std::max(a->max_tseg, it.t_hi - it.t_lo);
-    if (!P.items.empty() && ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl) > 227 * 1024) {
+    if (!P.items.empty() && ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl, P.axis_cap) > 227 * 1024) {
         delete a;
         return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
     }
     int bps = 0;
     if (!P.items.empty()) {
-        bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl));
+        bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl,
+                                                                                P.axis_cap));
         if (bps < 1) {
             delete a;
             return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
@@ -1319,7 +1320,7 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
     } else {
         CK(ism_backward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(a->d + a->L.o_items), n_items,
                                d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, ctl + 1, ctl + 2,
-                               a->max_tseg, a->grid_b, P.clamp, st));
+                               a->max_tseg, P.axis_cap, a->grid_b, P.clamp, st));
     }
     const int *dp[6];
     for (int k = 0; k < 6; k++) dp[k] = reinterpret_cast<const int *>(a->d + a->o_arr[k]);

@@ -37,6 +37,7 @@ struct BwdLaunch {
     int *status;
     int max_tseg;
     int pad;                  // g staging margin (>= taps reach)
+    int axis_cap;             // per-axis table entries (max over rooms of N0 + N1 + N2)
 };
 
 __device__ __forceinline__ float rcp_approx_b(float x) {
@@ -79,6 +80,12 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
     float *red = reinterpret_cast<float *>(ctl + 4);                 // [kBWarps][kGrad]
     // then [kGrad][kBThreads] per-thread gradient partials
     float *gs = red + (kBWarps + kBThreads) * kGrad;                 // staged dL/dh
+    // per-axis image terms of the current item (m < N0, then N1, then N2 entries):
+    //   tab[e]  = {v^2 hi, v^2 lo, v hi, (-b_lo)^e_lo (-b_hi)^e_hi}, as the forward kernel
+    //   tabd[e] = {(-b_lo)^e_lo, (-b_hi)^e_hi, e_lo (-b_lo)^(e_lo-1), e_hi (-b_hi)^(e_hi-1)}
+    // with e_lo = |c - r|, e_hi = |c| and b_lo, b_hi the axis' two walls
+    float4 *tab = reinterpret_cast<float4 *>(gs + ((P.max_tseg + 2 * P.pad + 3) & ~3));
+    float4 *tabd = tab + P.axis_cap;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // per-lane tap constants; one Fs per launch, so one window for every room: computed
@@ -145,6 +152,25 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
             __syncthreads();
             continue;
         }
+        // per-axis tables of this item (an image's squared distance is then two float-float
+        // additions, the same operations in the same order as in the forward kernel)
+        for (int e = tid; e < N0 + N1 + N2; e += kBThreads) {
+            const int a = e < N0 ? 0 : (e < N0 + N1 ? 1 : 2);
+            const int m = e - (a == 0 ? 0 : (a == 1 ? N0 : N0 + N1));
+            const int Na = a == 0 ? N0 : (a == 1 ? N1 : N2);
+            const float La = a == 0 ? L0 : (a == 1 ? L1 : L2);
+            const float sa = a == 0 ? sx : (a == 1 ? sy : sz), ra = a == 0 ? rx : (a == 1 ? ry : rz);
+            int ca, fa;
+            image_axis(m, Na, ca, fa);
+            const ff v = ff_add(ff_two_prod((float)(2 * ca), La), ff_two_sum(fa ? -sa : sa, -ra));
+            const ff sq = ff_sqr(v);
+            const int elo = abs(ca - fa), ehi = abs(ca);
+            const float plo = R.pw[2 * a][elo], phi = R.pw[2 * a + 1][ehi];
+            tab[e] = make_float4(sq.hi, sq.lo, v.hi, plo * phi);
+            tabd[e] = make_float4(plo, phi, elo > 0 ? (float)elo * R.pw[2 * a][elo - 1] : 0.0f,
+                                  ehi > 0 ? (float)ehi * R.pw[2 * a + 1][ehi - 1] : 0.0f);
+        }
+        __syncthreads();
         // Stage g over [t_lo - pad, t_hi + pad), zero outside this item's segment: copies
         // in flight while the first images' geometry is computed
         {
@@ -186,14 +212,8 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
                 int q, m2, m0, m1;
                 divmod_small(ii, N2, rN2, q, m2);
                 divmod_small(q, N1, rN1, m0, m1);
-                int c0, r0, c1, r1, c2, r2;
-                image_axis(m0, N0, c0, r0);
-                image_axis(m1, N1, c1, r1);
-                image_axis(m2, N2, c2, r2);
-                const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
-                const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
-                const ff v2 = ff_add(ff_two_prod((float)(2 * c2), L2), ff_two_sum(r2 ? -sz : sz, -rz));
-                const ff d2 = ff_add(ff_add(ff_sqr(v0), ff_sqr(v1)), ff_sqr(v2));
+                const float4 t0 = tab[m0], t1 = tab[N0 + m1], t2 = tab[N0 + N1 + m2];
+                const ff d2 = ff_add(ff_add(ff{t0.x, t0.y}, ff{t1.x, t1.y}), ff{t2.x, t2.y});
                 // approximate distance first: far images stop here
                 const float rs0 = rsqrtf(d2.hi);
                 const float s0 = d2.hi * rs0;
@@ -288,25 +308,20 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
                 int q, m2, m0, m1;
                 divmod_small(i, N2, rN2, q, m2);
                 divmod_small(q, N1, rN1, m0, m1);
-                int cc[3], rr[3];
-                image_axis(m0, N0, cc[0], rr[0]);
-                image_axis(m1, N1, cc[1], rr[1]);
-                image_axis(m2, N2, cc[2], rr[2]);
-                const float src[3] = {sx, sy, sz}, rcv[3] = {rx, ry, rz}, L[3] = {L0, L1, L2};
-                float v[3];
-                int e[6];
-                float pwv[6];
+                const int mi[3] = {m0, N0 + m1, N0 + N1 + m2};
+                const int rr[3] = {(m0 - N0 / 2) & 1, (m1 - N1 / 2) & 1, (m2 - N2 / 2) & 1};
+                float v[3], A[3];
+                float4 dp[3];
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    v[d] = (float)(2 * cc[d]) * L[d] + (rr[d] ? -src[d] : src[d]) - rcv[d];
-                    e[2 * d] = abs(cc[d] - rr[d]);
-                    e[2 * d + 1] = abs(cc[d]);
-                    pwv[2 * d] = __ldg(&R.pw[2 * d][e[2 * d]]);
-                    pwv[2 * d + 1] = __ldg(&R.pw[2 * d + 1][e[2 * d + 1]]);
+                    const float4 t = tab[mi[d]];
+                    v[d] = t.z;
+                    A[d] = t.w;
+                    dp[d] = tabd[mi[d]];
                 }
                 const float d2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
                 const float inv_d = rsqrtf(d2);
-                const float att = pwv[0] * pwv[1] * pwv[2] * pwv[3] * pwv[4] * pwv[5];
+                const float att = A[0] * A[1] * A[2];
                 float Ds = 1.f, Dm = 1.f, cs_ = 0.f, cm = 0.f;
                 float ms[3] = {0.f, 0.f, 0.f};   // mirrored source axis
                 if (spkr != P_OMNI) {
@@ -323,17 +338,14 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
                 const float amp = att * Ds * Dm * g0;
                 const float GA = wga[j];
                 const float GT = -amp * wgb[j];                      // dL/dtau
-                // beta: d att / d beta_w = -e_w (-beta_w)^(e_w - 1) * (other five factors)
+                // beta: d att / d beta_w = -e_w (-beta_w)^(e_w - 1) * (the other five factors);
+                // per axis the walls' factors are (-b_lo)^e_lo and (-b_hi)^e_hi
+                const float dA = GA * Ds * Dm * g0;   // dL / d att
 #pragma unroll
-                for (int w = 0; w < 6; w++) {
-                    if (e[w] > 0) {
-                        float others = 1.0f;
-#pragma unroll
-                        for (int u = 0; u < 6; u++)
-                            if (u != w) others *= pwv[u];
-                        const float datt = -(float)e[w] * __ldg(&R.pw[w][e[w] - 1]) * others;
-                        acc(w) = fmaf(GA * Ds * Dm * g0, datt, acc(w));
-                    }
+                for (int d = 0; d < 3; d++) {
+                    const float rest = dA * A[(d + 1) % 3] * A[(d + 2) % 3];
+                    acc(2 * d) = fmaf(-rest * dp[d].y, dp[d].z, acc(2 * d));
+                    acc(2 * d + 1) = fmaf(-rest * dp[d].x, dp[d].w, acc(2 * d + 1));
                 }
                 // d amp / d v and d tau / d v
                 const float ds = pattern_slope(spkr), dm = pattern_slope(mic);
@@ -426,10 +438,11 @@ __global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
     }
 }
 
-size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad) {
+size_t ism_backward_smem_bytes(int tpl, int max_tseg, int pad, int axis_cap) {
     (void)tpl;
     return kBThreads * (2 * sizeof(float4) + 2 * sizeof(float)) + 4 * sizeof(int) +
-           (kBWarps + kBThreads) * kGrad * sizeof(float) + (size_t)(max_tseg + 2 * pad) * sizeof(float);
+           (kBWarps + kBThreads) * kGrad * sizeof(float) +
+           (size_t)((max_tseg + 2 * pad + 3) & ~3) * sizeof(float) + (size_t)axis_cap * 2 * sizeof(float4);
 }
 
 template <int TPL, bool CLAMP>
@@ -448,15 +461,16 @@ static cudaError_t bwd_tpl(const BwdLaunch &p, int grid, size_t smem, cudaStream
 cudaError_t ism_backward_launch(int tpl, const RoomDesc *rooms, const IsmItem *items, int n_items,
                                 const float *pos_src, const float *pos_rcv, const float *orv_src,
                                 const float *orv_rcv, const float *grad, float *item_grad,
-                                int *work_counter, int *status, int max_tseg, int grid, int clamp,
-                                cudaStream_t st) {
+                                int *work_counter, int *status, int max_tseg, int axis_cap, int grid,
+                                int clamp, cudaStream_t st) {
     BwdLaunch p;
+    p.axis_cap = axis_cap;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
     p.grad = grad; p.item_grad = item_grad; p.work_counter = work_counter; p.status = status;
     p.max_tseg = max_tseg;
     p.pad = 64 * tpl;   // >= 2 * 32 * TPL reach of the taps on either side
-    size_t smem = ism_backward_smem_bytes(tpl, max_tseg, p.pad);
+    size_t smem = ism_backward_smem_bytes(tpl, max_tseg, p.pad, axis_cap);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     // taps beyond |x| < Tw/2 exist only when the window does not fill the lanes exactly
