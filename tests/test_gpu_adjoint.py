@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 TOL = 2e-4
 
 
-def _setup(seed, spkr="card", mic="hypcard", ns=2, nr=3, nb=(5, 6, 7), T=0.06, room=(4.0, 3.5, 2.8)):
+def _setup(seed, spkr="card", mic="hypcard", ns=2, nr=3, nb=(5, 6, 7), T=0.06, room=(4.0, 3.5, 2.8), fs=16000.0):
     rng = np.random.default_rng(seed)
     room = np.array(room)
     ps = (0.5 + rng.random((ns, 3)) * (room - 1.0)).astype(np.float32)
@@ -24,10 +24,10 @@ def _setup(seed, spkr="card", mic="hypcard", ns=2, nr=3, nb=(5, 6, 7), T=0.06, r
     os_ = rng.standard_normal((ns, 3)).astype(np.float32)
     or_ = rng.standard_normal((nr, 3)).astype(np.float32)
     beta = rng.uniform(0.6, 0.95, 6).astype(np.float32)
-    n = oracle.n_samples(T, 16000.0)
+    n = oracle.n_samples(T, fs)
     g = rng.standard_normal((ns, nr, n))
     return dict(room=room.astype(np.float32), ps=ps, pr=pr, os=os_, orv=or_, beta=beta, nb=list(nb),
-                T=T, n=n, g=g, spkr=spkr, mic=mic)
+                T=T, n=n, g=g, spkr=spkr, mic=mic, fs=fs)
 
 
 def _ours(c):
@@ -37,7 +37,7 @@ def _ours(c):
     beta, ps, pr = t(c["beta"]), t(c["ps"]), t(c["pr"])
     os_ = t(c["os"]) if c["spkr"] != "omni" else None
     or_ = t(c["orv"]) if c["mic"] != "omni" else None
-    h = simulate_rir_torch(c["room"], beta, ps, pr, c["nb"], c["T"], 16000.0, spkr_pattern=c["spkr"],
+    h = simulate_rir_torch(c["room"], beta, ps, pr, c["nb"], c["T"], c["fs"], spkr_pattern=c["spkr"],
                            mic_pattern=c["mic"], orV_src=os_, orV_rcv=or_)
     loss = (h.double() * torch.tensor(c["g"], device="cuda")).sum()
     loss.backward()
@@ -54,7 +54,7 @@ def _ref(c):
     from torch_ism_ref import early_part
     t = lambda a: torch.tensor(np.asarray(a, dtype=np.float64), requires_grad=True)
     beta, ps, pr, os_, or_ = t(c["beta"]), t(c["ps"]), t(c["pr"]), t(c["os"]), t(c["orv"])
-    h = early_part(c["room"], beta, ps, pr, c["nb"], c["n"], 16000.0, spkr=c["spkr"], mic=c["mic"],
+    h = early_part(c["room"], beta, ps, pr, c["nb"], c["n"], c["fs"], spkr=c["spkr"], mic=c["mic"],
                    orV_src=os_, orV_rcv=or_)
     loss = (h * torch.tensor(c["g"])).sum()
     loss.backward()
@@ -292,3 +292,16 @@ def test_backward_after_two_forwards_uses_each_calls_beta(built):
     one2, = grads([(b2, g2)])
     assert np.array_equal(both[0], one1) and np.array_equal(both[1], one2)
     assert not np.allclose(one1, one2)
+
+
+@pytest.mark.parametrize("fs", [22050.0, 48000.0])
+def test_gradients_at_other_sample_rates(built, fs):
+    """Windows that do not fill the lanes exactly (Tw = 176 and 384 samples: 8 and 12 taps
+    per lane, taps beyond |x| < Tw/2 masked) against the FP64 reference."""
+    c = _setup(43, "card", "hypcard", nb=(4, 5, 6), T=0.05, fs=fs)
+    ours, h = _ours(c)
+    ref, href = _ref(c)
+    assert rel_l2(h.detach().cpu().numpy(), href) < 1e-5
+    for k in ours:
+        e = rel_l2(ours[k], ref[k])
+        assert e < TOL, (fs, k, e)

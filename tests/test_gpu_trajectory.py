@@ -27,9 +27,11 @@ def _direct(seg, rir):
 
 @pytest.mark.parametrize("P,S,R,L", [(3, 5, 2, 4), (7, 401, 3, 257), (4, 1000, 2, 3000),
                                      (2, 400, 8, 12800), (2, 3000, 2, 14000), (1, 1, 1, 1),
-                                     (5, 64, 1, 65)])
+                                     (5, 64, 1, 65), (3, 700, 1, 1500), (5, 400, 3, 12800)])
 def test_gpu_conv_matches_direct(built, P, S, R, L):
-    """Covers shared-memory FFTs (N <= 16384) and global-scratch FFTs (N = 32768)."""
+    """Covers shared-memory FFTs (N <= 16384) and global-scratch FFTs (N = 32768); the
+    register kernels transform two rows per block, so odd row counts (a last block with
+    one row) and pairs of rows from different points are included."""
     from gpurir_gb300.trajectory import gpu_conv
     rng = np.random.default_rng(P * 1000 + S)
     seg = rng.standard_normal((P, S)).astype(np.float32)
