@@ -359,3 +359,21 @@ def test_one_shot_adjoint_matches_torch_batch(built):
     for ours, ref in ((gb, beta.grad), (gs, ps.grad), (gq, pr.grad)):
         ref = ref.cpu().numpy()
         assert rel_l2(ours, ref) < 1e-6, rel_l2(ours, ref)
+
+
+def test_plan_reuse_across_mode_switches(built):
+    """Same shapes, the evaluation mode switched between calls on one simulator: each call
+    matches a fresh simulator in that mode (the reused plan is keyed by the mode)."""
+    import gpurir_gb300 as G
+    rng = np.random.default_rng(29)
+    room, nb, T = [4.0, 5.0, 3.0], [6, 6, 6], 0.1
+    ps, pr = _rand_inside(rng, 2, room, 0.5), _rand_inside(rng, 3, room, 0.5)
+    args = (room, [0.8] * 6, ps, pr, None, None, 0, 0, nb, T, T, 16000.0)
+    sim = _sim()
+    fresh = {m: G.Simulator(mixed_precision=(m == "mp"), lut=(m == "lut"), seed=1234) for m in ("fp32", "mp", "lut")}
+    for mode in ("fp32", "lut", "fp32", "mp", "lut"):
+        sim.activate_lut(mode == "lut")
+        sim.activate_mixed_precision(mode == "mp")
+        got = sim.simulate_rir(*args)
+        want = fresh[mode].simulate_rir(*args)
+        assert np.array_equal(got, want), mode
