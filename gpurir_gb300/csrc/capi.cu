@@ -58,7 +58,7 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
                             const float2 *Sg, float *out, long out_ld, float2 *scratch, int grid,
                             cudaStream_t st);
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
-                       int L, long n_out, double *out, cudaStream_t st);
+                       int L, long n_out, int uni_w, double *out, cudaStream_t st);
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
 cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
                                   int n_items, const float *pos_src, const float *pos_rcv, unsigned char *skip,
@@ -1498,8 +1498,13 @@ static int trajectory_core(gpurir_sim *s, const float *d_seg, int n_pts, int seg
     const long n = (long)seg_len + rir_len - 1;
     float *conv = reinterpret_cast<float *>(s->d_conv + C.o_conv);
     if ((rc = run_conv(s, C, d_seg, n_pts, seg_len, d_rir, n_rcv, rir_len, conv, conv_ld(n), st))) return rc;
+    // segments back to back with one width (the default segmentation): the overlap-add
+    // finds each sample's points by division instead of searching the window table
+    int uni_w = n_pts > 0 ? w_ini[1] - w_ini[0] : 0;
+    for (int p = 0; p < n_pts && uni_w > 0; p++)
+        if (w_ini[p] != p * uni_w || w_ini[p + 1] - w_ini[p] != uni_w) uni_w = 0;
     CK(ola_launch(conv, conv_ld(n), dwin, dwin + n_pts + 1, n_pts, n_rcv, rir_len,
-                  (long)w_ini[n_pts] + rir_len - 1, d_out, st));
+                  (long)w_ini[n_pts] + rir_len - 1, uni_w, d_out, st));
     CK(cudaEventRecord(s->conv_busy, st));
     s->conv_recorded = true;
     return GPURIR_OK;

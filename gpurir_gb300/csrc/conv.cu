@@ -657,21 +657,30 @@ static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S,
 // increasing p, of conv[p][r][t - w_ini[p]] for 0 <= t - w_ini[p] < w_len[p] + L - 1.
 // Compensated FP32 sum (two-sum), written as float64.
 __global__ void ola_kernel(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P,
-                           int R, int L, long n_out, double *out) {
+                           int R, int L, long n_out, int uni_w, double *out) {
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;   // consecutive t: coalesced reads
     const int r = blockIdx.y;
     if (t >= n_out) return;
     // points whose filtered segment covers t: lo = first p with w_ini[p] + w_len[p] + L - 1 > t,
-    // hi = first p with w_ini[p] > t (w_ini increasing, w_ini[p] + w_len[p] = w_ini[p + 1])
-    int lo = 0, hi = P;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if ((long)w_ini[mid] + w_len[mid] + L - 1 > t) hi = mid; else lo = mid + 1;
-    }
-    int e = lo, e_hi = P;
-    while (e < e_hi) {
-        const int mid = (e + e_hi) >> 1;
-        if ((long)w_ini[mid] > t) e_hi = mid; else e = mid + 1;
+    // e = first p with w_ini[p] > t (w_ini increasing, w_ini[p] + w_len[p] = w_ini[p + 1])
+    int lo, e;
+    if (uni_w > 0) {   // w_ini[p] = p W, w_len[p] = W: both bounds by division
+        const long a = t - (uni_w + L - 1);   // p W + W + L - 1 > t  <=>  p > a / W
+        lo = a < 0 ? 0 : (int)min((long)P, a / uni_w + 1);
+        e = (int)min((long)P, t / uni_w + 1);
+    } else {
+        lo = 0;
+        int hi = P;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if ((long)w_ini[mid] + w_len[mid] + L - 1 > t) hi = mid; else lo = mid + 1;
+        }
+        e = lo;
+        int e_hi = P;
+        while (e < e_hi) {
+            const int mid = (e + e_hi) >> 1;
+            if ((long)w_ini[mid] > t) e_hi = mid; else e = mid + 1;
+        }
     }
     // every p in [lo, e) contributes conv[p][r][t - w_ini[p]]: independent loads, then the
     // compensated sum in increasing p
@@ -765,11 +774,11 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
 }
 
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
-                       int L, long n_out, double *out, cudaStream_t st) {
+                       int L, long n_out, int uni_w, double *out, cudaStream_t st) {
     if (n_out <= 0 || R <= 0) return cudaSuccess;
     if (R > 65535) return cudaErrorInvalidValue;
     dim3 grid((unsigned)((n_out + 255) / 256), (unsigned)R);
-    ola_kernel<<<grid, 256, 0, st>>>(conv, conv_ld, w_ini, w_len, P, R, L, n_out, out);
+    ola_kernel<<<grid, 256, 0, st>>>(conv, conv_ld, w_ini, w_len, P, R, L, n_out, uni_w, out);
     return cudaGetLastError();
 }
 
