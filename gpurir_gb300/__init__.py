@@ -25,7 +25,7 @@ from ._lib import GpuRirError
 
 __all__ = ["polar_patterns", "beta_SabineEstimation", "att2t_SabineEstimator", "t2n",
            "simulateRIR", "simulateTrajectory", "activateMixedPrecision", "activateLUT",
-           "seed", "set_noise", "GpuRirError"]
+           "activateReferenceDelays", "seed", "set_noise", "GpuRirError"]
 
 # gpuRIR/__init__.py:13-20 (numbering of src/gpuRIR_cuda.h:2-8)
 polar_patterns = {
@@ -107,12 +107,14 @@ def t2n(T, rooms_sz, c=343.0):
 class Simulator:
     """Owns one gpurir_sim handle of the C ABI (one CUDA stream + workspace)."""
 
-    def __init__(self, mixed_precision=False, lut=False, seed=1234):
+    def __init__(self, mixed_precision=False, lut=False, seed=1234, reference_delays=False):
         self._L = _lib.load()
         h = ctypes.c_void_p()
         _lib.check(self._L.gpurir_create(int(mixed_precision), int(lut), int(seed),
                                          ctypes.byref(h)), "gpurir_create")
         self._h = h
+        if reference_delays:
+            self.activate_reference_delays(True)
 
     def __del__(self):
         L = getattr(self, "_L", None)
@@ -137,10 +139,19 @@ class Simulator:
                    "activate_lut")
         return bool(st.value)
 
+    def activate_reference_delays(self, activate):
+        """Round image delays in float32 as gpuRIR's calcAmpTau_kernel does
+        (src/gpuRIR_cuda.cu:336-369) instead of computing them exactly."""
+        st = ctypes.c_int()
+        _lib.check(self._L.gpurir_set_reference_delays(self._h, int(bool(activate)), ctypes.byref(st)),
+                   "reference_delays")
+        return bool(st.value)
+
     def modes(self):
-        mp, lut = ctypes.c_int(), ctypes.c_int()
+        mp, lut, rd = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _lib.check(self._L.gpurir_get_modes(self._h, ctypes.byref(mp), ctypes.byref(lut)), "modes")
-        return dict(mixed_precision=bool(mp.value), lut=bool(lut.value))
+        _lib.check(self._L.gpurir_get_reference_delays(self._h, ctypes.byref(rd)), "modes")
+        return dict(mixed_precision=bool(mp.value), lut=bool(lut.value), reference_delays=bool(rd.value))
 
     def set_seed(self, seed, call_counter=0):
         _lib.check(self._L.gpurir_set_seed(self._h, int(seed), int(call_counter)), "set_seed")
@@ -278,6 +289,15 @@ def activateMixedPrecision(activate=True):
 def activateLUT(activate=True):
     """Lookup-table sinc evaluation (gpuRIR/__init__.py:234-243).  Turns mixed precision off."""
     simulator().activate_lut(activate)
+
+
+def activateReferenceDelays(activate=True):
+    """Image delays rounded in float32 step by step as gpuRIR's kernel rounds them
+    (src/gpuRIR_cuda.cu:336-369), so that outputs match gpuRIR's own build instead
+    of the exact sum (gpuRIR's delays are up to ~4e-4 samples off at 0.3 s).  Off
+    by default; independent of the mixed-precision and lookup-table switches.
+    gpuRIR has no such switch: its delays are always the float32 ones."""
+    simulator().activate_reference_delays(activate)
 
 
 def _marshal_simulate_args(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,

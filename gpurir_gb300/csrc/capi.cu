@@ -91,6 +91,7 @@ static void free_plan_cache(PlanCache *c);
 
 struct gpurir_sim {
     int mp = 0, lut = 0;
+    int ref_delay = 0;   // image delays in the reference's float32 arithmetic (RoomDesc::ref_delay)
     uint64_t seed = 1234, calls = 0;
     int noise = GPURIR_NOISE_LOGISTIC;
     int device = 0, num_sms = 0;
@@ -215,6 +216,19 @@ extern "C" int gpurir_activate_lut(gpurir_sim *s, int activate, int *state) {
     return GPURIR_OK;
 }
 
+extern "C" int gpurir_set_reference_delays(gpurir_sim *s, int activate, int *state) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    s->ref_delay = activate ? 1 : 0;
+    if (state) *state = s->ref_delay;
+    return GPURIR_OK;
+}
+
+extern "C" int gpurir_get_reference_delays(gpurir_sim *s, int *state) {
+    if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
+    if (state) *state = s->ref_delay;
+    return GPURIR_OK;
+}
+
 extern "C" int gpurir_get_modes(gpurir_sim *s, int *mp, int *lut) {
     if (!s) return fail(GPURIR_ERR_INVALID, "NULL handle");
     if (mp) *mp = s->mp;
@@ -313,6 +327,7 @@ static int build_room(RoomDesc &R, const float room[3], const float beta[6], con
                ((1.0f - beta[4] * beta[4]) + (1.0f - beta[5] * beta[5])) * room[0] * room[1];
     R.T60 = 0.161f * (room[0] * room[1] * room[2]) / Sa;
     R.fs = Fs;
+    R.c = c;
     R.pow_n = pow_table_len(nb);
     if (R.pow_n > kPowMax) return fail(GPURIR_ERR_INVALID, "nb_img too large for the reflection tables");
     // (-beta)^k by repeated FP64 products rounded to float32: the room-table kernel of
@@ -696,6 +711,7 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
                           const float *orV_rcv, float *out, long long out_elems, bool host_io,
                           cudaStream_t st, const float *d_beta = nullptr) {
     int rc;
+    for (RoomDesc &r : R) r.ref_delay = s->ref_delay;
     std::vector<double> key = plan_key(s, R, host_io, out_elems);
     const bool hit = s->pcache && s->pcache->key == key;
     if (!hit) {
@@ -980,6 +996,7 @@ extern "C" int gpurir_batch_create(gpurir_sim *s, int n_rooms, const gpurir_room
     long long tot;
     int rc = build_batch(n_rooms, rooms, Fs, c, R, ns, nr, tot);
     if (rc) return rc;
+    for (RoomDesc &r : R) r.ref_delay = s->ref_delay;
     Plan P;
     if ((rc = plan_rooms(s, R, P))) return rc;
     const long M = (long)P.rirs.size();

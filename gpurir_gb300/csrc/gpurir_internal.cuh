@@ -36,7 +36,9 @@ struct RoomDesc {
     float beta[6];         // wall reflection coefficients (tail / adjoint)
     long long out_off;     // element offset of the room's first RIR row in the output
     int pow_n;             // valid entries per wall in the power table
-    int pad_[3];
+    float c;               // speed of sound [m/s] as the caller gave it
+    int ref_delay;         // 1: delays in the reference's float32 arithmetic (ref_tau)
+    int pad_;
     float pw[6][kPowMax];  // pw[w][k] = (-beta[w])^k, rounded from FP64
 };
 
@@ -237,6 +239,37 @@ __device__ __forceinline__ bool images_miss_segment(const float L[3], const int 
     const float tau_lo = sqrtf(lo2) * fs_c, tau_hi = sqrtf(hi2) * fs_c;
     const float margin = 2.0f + 1e-5f * tau_hi;
     return tau_hi < (float)t_lo - H - margin || tau_lo > (float)t_hi + H + margin;
+}
+
+// ---------------------------------------------------------------------------
+// Reference-delay model: the image delay exactly as gpuRIR's calcAmpTau_kernel
+// rounds it in float32 (src/gpuRIR_cuda.cu:336-367), for callers that want the
+// reference's output rather than the exact sum.  Each step is an explicit
+// round-to-nearest intrinsic so that no contraction of ours can change it.
+// ---------------------------------------------------------------------------
+// One component of the receiver -> image vector (:337, :353): the cluster offset
+// (2 clust) L rounded, plus or minus the source coordinate rounded, minus the
+// receiver coordinate rounded.
+__device__ __forceinline__ float ref_axis_component(int clust, int refl, float L, float s, float r) {
+    const float cp = __fmul_rn((float)(2 * clust), L);
+    return __fsub_rn(__fadd_rn(cp, refl ? -s : s), r);
+}
+
+// Squared distance from the three components as the reference build forms it.
+// The reference's loop `dist += vec[d] * vec[d]` (:354) is contracted by the
+// compiler in two ways, depending on which version of its loop runs: with both
+// patterns omni, one FMA per component in axis order; with a directional source
+// or receiver, x^2 + y^2 rounded separately and then one FMA for z.  Both were
+// identified bit for bit against the delays the reference's own kernel wrote.
+__device__ __forceinline__ float ref_dist2(float v0, float v1, float v2, bool directional) {
+    if (directional) return __fmaf_rn(v2, v2, __fadd_rn(__fmul_rn(v0, v0), __fmul_rn(v1, v1)));
+    return __fmaf_rn(v2, v2, __fmaf_rn(v1, v1, __fmul_rn(v0, v0)));
+}
+
+// Delay in samples from the squared distance: sqrtf, then `dist / c * Fs` (:366)
+// with IEEE division and multiplication.
+__device__ __forceinline__ float ref_tau(float d2, float c, float fs) {
+    return __fmul_rn(__fdiv_rn(__fsqrt_rn(d2), c), fs);
 }
 
 // Directivity gain, src/gpuRIR_cuda.cu:132-147, with the cosine already formed.

@@ -250,6 +250,9 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const float H = R.H;
         const float inv_h = 1.0f / H;
         const float rN1 = 1.0f / (float)N1, rN2 = 1.0f / (float)N2;
+        // delays in the reference's float32 arithmetic instead of the exact ones
+        const bool ref_delay = R.ref_delay != 0;
+        const bool ref_dir = R.spkr != P_OMNI || R.mic != P_OMNI;
         const bool small_phi = inv_h <= 0.0625f;   // window angle f / H <= 1/16: polynomials
         // per-axis terms once per item: an image's squared distance is then two
         // float-float additions (the same operations, in the same order, as per image)
@@ -269,10 +272,15 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 const float ra = a == 0 ? P.pos_rcv[3 * it.rcv] : (a == 1 ? P.pos_rcv[3 * it.rcv + 1] : P.pos_rcv[3 * it.rcv + 2]);
                 int ca, fa;
                 image_axis(m, Na, ca, fa);
-                const ff v = ff_add(ff_two_prod((float)(2 * ca), La), ff_two_sum(fa ? -sa : sa, -ra));
-                const ff sq = ff_sqr(v);
                 const float att = R.pw[2 * a][abs(ca - fa)] * R.pw[2 * a + 1][abs(ca)];
-                tab[e] = make_float4(sq.hi, sq.lo, v.hi, att);
+                if (ref_delay) {   // the reference's float32 component; its square only bounds
+                    const float v = ref_axis_component(ca, fa, La, sa, ra);
+                    tab[e] = make_float4(v * v, 0.0f, v, att);
+                } else {
+                    const ff v = ff_add(ff_two_prod((float)(2 * ca), La), ff_two_sum(fa ? -sa : sa, -ra));
+                    const ff sq = ff_sqr(v);
+                    tab[e] = make_float4(sq.hi, sq.lo, v.hi, att);
+                }
             }
             __syncthreads();
         }
@@ -358,6 +366,12 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                         d2 = ff_add(ff_add(ff{t0.x, t0.y}, ff{t1.x, t1.y}), ff{t2.x, t2.y});
                         v0h = t0.z; v1h = t1.z; v2h = t2.z;
                         att_t = t0.w * t1.w * t2.w;
+                        if (ref_delay) d2 = ff{ref_dist2(v0h, v1h, v2h, ref_dir), 0.0f};
+                    } else if (ref_delay) {
+                        v0h = ref_axis_component(c0, r0, L0, sx, rx);
+                        v1h = ref_axis_component(c1, r1, L1, sy, ry);
+                        v2h = ref_axis_component(c2, r2, L2, sz, rz);
+                        d2 = ff{ref_dist2(v0h, v1h, v2h, ref_dir), 0.0f};
                     } else {
                         const ff v0 = ff_add(ff_two_prod((float)(2 * c0), L0), ff_two_sum(r0 ? -sx : sx, -rx));
                         const ff v1 = ff_add(ff_two_prod((float)(2 * c1), L1), ff_two_sum(r1 ? -sy : sy, -ry));
@@ -379,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                         // (the residual by FMA is exact to ~1e-14 of d2)
                         float inv_d;
                         const ff dist = ff_dist_newton(d2, rs0, s0, inv_d);
-                        const ff tau = ff_mul(dist, kfs);
+                        const ff tau = ref_delay ? ff{ref_tau(d2.hi, R.c, R.fs), 0.0f} : ff_mul(dist, kfs);
                         float amp = att * (0.0795774715459476679f * inv_d);   // 1/(4 pi dist)
                         if (spkr != P_OMNI) {
                             // doa = image -> receiver = -vec; axis mirrored per reflection (:357-362)

@@ -10,9 +10,15 @@
 // descriptor, the work-item table, the work counter and the status word -- is
 // the fixed array below, present on every GPU that loads the library until the
 // process exits.  The kernel is the fused forward kernel of ism_forward.cu.
+//
+// The forward kernel can flag an inconsistent work item in the status word of
+// the scratch, but the items here are built by noalloc_prepare_kernel from
+// sizes the host has already checked, so no flag is ever raised on this path;
+// the word is cleared by the next call and not reported.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "gpurir_internal.cuh"
 #include "../../include/gpurir_gb300.h"
@@ -44,9 +50,47 @@ constexpr size_t kNoAllocBytes = kNoAllocCtl + kNoAllocRoom + (size_t)kNoAllocMa
 // (about 390 KB).  Shared by every call on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Device address of the scratch, looked up once per device with that device current.
+// Device address of the scratch per device, with the id of the CUDA context it
+// was looked up in.  A device reset destroys the context and the module with it,
+// and the array may then live at another address: a call whose current context
+// differs from the cached one looks the address up again (cudaGetSymbolAddress
+// allocates nothing; on the first call in a context it may load the module).
+// The cache is guarded by a mutex (no allocation either).
 constexpr int kMaxDevices = 64;
-static unsigned char *g_scratch_ptr[kMaxDevices];
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    unsigned char *ptr;
+};
+static ScratchSlot g_scratch[kMaxDevices];
+static std::mutex g_scratch_mu;
+
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+static CtxGetIdFn g_ctx_get_id = nullptr;
+static std::once_flag g_ctx_fns_once;
+
+// Id of the current CUDA context (0: none current, or the driver lacks the query).
+static unsigned long long current_context_id() {
+    std::call_once(g_ctx_fns_once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    });
+    if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx) return 0;
+    if (g_ctx_get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 static int scratch_for_current_device(unsigned char **out) {
     int dev = 0;
@@ -54,15 +98,19 @@ static int scratch_for_current_device(unsigned char **out) {
     if (e != cudaSuccess) return set_last_error(GPURIR_ERR_CUDA, "gpurir_simulate_ism_noalloc: cudaGetDevice failed");
     if (dev < 0 || dev >= kMaxDevices)
         return set_last_error(GPURIR_ERR_UNSUPPORTED, "gpurir_simulate_ism_noalloc: device index above 63");
-    if (!g_scratch_ptr[dev]) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    unsigned long long id = current_context_id();
+    ScratchSlot &slot = g_scratch[dev];
+    if (id == 0 || !slot.ptr || slot.ctx_id != id) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return set_last_error(GPURIR_ERR_CUDA,
                                   "gpurir_simulate_ism_noalloc: cudaGetSymbolAddress of the scratch failed");
-        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+        slot.ptr = static_cast<unsigned char *>(p);
+        slot.ctx_id = current_context_id();   // the lookup made the primary context current
     }
-    *out = g_scratch_ptr[dev];
+    *out = slot.ptr;
     return GPURIR_OK;
 }
 
@@ -138,7 +186,8 @@ extern "C" int gpurir_simulate_ism_noalloc(const float room_sz[3], const float b
     n_seg = (R.n_ism + tseg - 1) / tseg;
     if (M * n_seg > kNoAllocMaxItems)
         return set_last_error(GPURIR_ERR_INVALID,
-                              "gpurir_simulate_ism_noalloc: RIRs x segments above 8192 (fixed scratch limit)");
+                              "gpurir_simulate_ism_noalloc: RIRs x segments above 8192 (fixed scratch limit; "
+                              "long RIRs are cut into several segments)");
     const int nsub = (int)((tseg + sub - 1) / sub);
     const int tw = (int)std::lround(2.0 * R.H);
     const size_t smem = ism_forward_smem_bytes(tpl, em, nsub, 0, tw);

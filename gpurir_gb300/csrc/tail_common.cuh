@@ -18,6 +18,13 @@ constexpr int kPowerThreads = 512;
 // Direct-path delay in samples, the float-float arithmetic the ISM kernel
 // applies to the image with clust = refl = 0 (src/gpuRIR_cuda.cu:368-369).
 __device__ __forceinline__ float direct_tau(const RoomDesc &R, const float *ps, const float *pr) {
+    if (R.ref_delay) {   // the reference's float32 tau_dp (:368-369)
+        const float d2 = ref_dist2(ref_axis_component(0, 0, R.L[0], ps[0], pr[0]),
+                                   ref_axis_component(0, 0, R.L[1], ps[1], pr[1]),
+                                   ref_axis_component(0, 0, R.L[2], ps[2], pr[2]),
+                                   R.spkr != P_OMNI || R.mic != P_OMNI);
+        return ref_tau(d2, R.c, R.fs);
+    }
     ff v0 = ff_two_sum(ps[0], -pr[0]);
     ff v1 = ff_two_sum(ps[1], -pr[1]);
     ff v2 = ff_two_sum(ps[2], -pr[2]);

@@ -65,6 +65,21 @@ int gpurir_activate_lut(gpurir_sim *sim, int activate, int *state);
 /* Read the flags. */
 int gpurir_get_modes(gpurir_sim *sim, int *mixed_precision, int *lookup_table);
 
+/* Delay model of the image sources.  Off (default): each delay is the exact
+ * distance * Fs / c, to ~1e-10 samples.  On: the delay is rounded in float32
+ * step by step as gpuRIR's calcAmpTau_kernel forms it (src/gpuRIR_cuda.cu:
+ * 336-369: cluster offset, receiver->image components, squared distance,
+ * sqrtf, dist / c * Fs), and the direct-path delay of the diffuse tail's
+ * envelope likewise, so that the output matches the reference build's up to
+ * the rounding of the tap arithmetic; the reference's delays are up to ~4e-4
+ * samples off the exact ones at 0.3 s.  Applies to every mode (FP32, mixed
+ * precision, lookup table) and to the simulate and batch entries of `sim`; the
+ * adjoint entries always differentiate the exact model.  The reference has no
+ * such switch (its delays are always the float32 ones).  *state receives the
+ * resulting flag (may be NULL). */
+int gpurir_set_reference_delays(gpurir_sim *sim, int activate, int *state);
+int gpurir_get_reference_delays(gpurir_sim *sim, int *state);
+
 /* Noise transform of the tail (GPURIR_NOISE_*), and the (seed, call counter)
  * pair that keys it.  The counter advances by one per simulate call. */
 int gpurir_set_noise(gpurir_sim *sim, int noise_kind);
@@ -227,15 +242,23 @@ int gpurir_trajectory(gpurir_sim *sim, const float *segments, int n_pts, int seg
  * real-time audio threads (cudaMalloc may block on a device synchronisation),
  * hosts with a fixed device-memory budget, work recorded under global stream
  * capture.  The kernel's scratch is a fixed ~390 KB array in this library,
- * held on every GPU that loads it until the process exits; calls are limited to
- * 8192 RIRs x segments (M_src * M_rcv <= 8192) and fail with GPURIR_ERR_INVALID
- * beyond.  Computes the image-source part only, as gpurir_simulate_rir_device
- * with Tdiff = Tmax = T: d_rir_out is [M_src][M_rcv][gpurir_n_samples(T, Fs)].
- * The first call on a device looks up the scratch address (cudaGetSymbolAddress);
- * make it before any stream capture.  Host arguments are copied from pageable
- * memory, so the call waits for earlier work on `stream`.  Every call shares the
- * one scratch array: calls whose GPU work overlaps (other streams, other host
- * threads) race and must be serialised by the caller. */
+ * held on every GPU that loads it until the process exits.  It holds 8192 work
+ * items: a call needs M_src * M_rcv * n_seg <= 8192, where n_seg is the number
+ * of segments an RIR is cut into, ceil(nSamples / S) with S the longest segment
+ * one block's shared memory holds (5120 samples at 16 kHz).  Example: at 16 kHz,
+ * T = 0.3 s (4800 samples, one segment) allows up to 8192 RIRs; T = 2 s (32000
+ * samples, 7 segments) up to 1170.  Larger calls fail with GPURIR_ERR_INVALID
+ * before anything is enqueued.  Computes the image-source part only, as
+ * gpurir_simulate_rir_device with Tdiff = Tmax = T: d_rir_out is
+ * [M_src][M_rcv][gpurir_n_samples(T, Fs)].  The first call on a device (and the
+ * first after a device reset) looks up the scratch address
+ * (cudaGetSymbolAddress); make it before any stream capture.  The call only
+ * enqueues two kernels on `stream` and returns without waiting: synchronise on
+ * the stream before reading d_rir_out.  Work items are built on the device from
+ * sizes checked here, so the kernel never rejects one and no device status is
+ * reported.  Every call shares the one scratch array: calls whose GPU work
+ * overlaps (other streams, other host threads) race and must be serialised by
+ * the caller. */
 int gpurir_simulate_ism_noalloc(const float room_sz[3], const float beta[6], const float *d_pos_src,
                                 int M_src, const float *d_pos_rcv, const float *d_orV_src,
                                 const float *d_orV_rcv, int spkr_pattern, int mic_pattern, int M_rcv,

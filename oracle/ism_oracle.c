@@ -135,6 +135,61 @@ void orc_amp_tau(const float room[3], const float beta[6],
 }
 
 /*
+ * Image delays as the reference build rounds them in float32 (the engine's
+ * reference-delay mode).  calcAmpTau_kernel, src/gpuRIR_cuda.cu:336-369:
+ * cluster offset (2 clust) * L, plus or minus the source coordinate, minus the
+ * receiver coordinate, each rounded; the squared distance as the compiled
+ * kernel contracts `dist += vec[d]*vec[d]` (one FMA per axis when both patterns
+ * are omni; x^2 + y^2 rounded separately, then an FMA for z, otherwise; matched
+ * bit for bit against the delays the reference kernel wrote,
+ * tests/golden/reference_kernels.npz); then sqrtf and dist / c * Fs.
+ * Compiled without contraction so that only the fmaf calls fuse.
+ *   tau    : [M_src][M_rcv][N0*N1*N2] float32
+ *   tau_dp : [M_src][M_rcv] float32
+ */
+__attribute__((optimize("fp-contract=off")))
+void orc_tau_ref_f32(const float room[3], const float *pos_src, int M_src, const float *pos_rcv,
+                     int M_rcv, int spkr_pattern, int mic_pattern, const int nb_img[3], float c,
+                     float Fs, float *tau, float *tau_dp)
+{
+    const int N0 = nb_img[0], N1 = nb_img[1], N2 = nb_img[2];
+    const long NN = (long)N0 * N1 * N2;
+    const int directional = spkr_pattern != P_OMNI || mic_pattern != P_OMNI;
+    for (int ms = 0; ms < M_src; ms++)
+    for (int mr = 0; mr < M_rcv; mr++)
+    for (int n0 = 0; n0 < N0; n0++)
+    for (int n1 = 0; n1 < N1; n1++)
+    for (int n2 = 0; n2 < N2; n2++) {
+        int n[3] = {n0, n1, n2}, N[3] = {N0, N1, N2};
+        float v[3];
+        int direct = 1;
+        for (int d = 0; d < 3; d++) {
+            int cl, rf;
+            orc_axis(n[d], N[d], &cl, &rf);
+            volatile float cp = (float)(2 * cl) * room[d];
+            volatile float a = cp + (rf ? -pos_src[ms * 3 + d] : pos_src[ms * 3 + d]);
+            v[d] = a - pos_rcv[mr * 3 + d];
+            direct = direct && cl == 0 && rf == 0;
+        }
+        float d2;
+        if (directional) {
+            volatile float xx = v[0] * v[0], yy = v[1] * v[1];
+            volatile float s = xx + yy;
+            d2 = fmaf(v[2], v[2], s);
+        } else {
+            volatile float xx = v[0] * v[0];
+            d2 = fmaf(v[2], v[2], fmaf(v[1], v[1], xx));
+        }
+        volatile float dist = sqrtf(d2);
+        volatile float q = dist / c;
+        float t = q * Fs;
+        long o = ((long)ms * M_rcv + mr) * NN + (long)n0 * N1 * N2 + (long)n1 * N2 + n2;
+        tau[o] = t;
+        if (direct) tau_dp[ms * M_rcv + mr] = t;
+    }
+}
+
+/*
  * Windowed-sinc accumulation of the early part.  Restates image_sample,
  * hanning_window and sinc (src/gpuRIR_cuda.cu:110-121) summed over images as
  * generateRIR_kernel/reduceRIR_kernel do (:377-413).  Terms outside

@@ -51,6 +51,9 @@ def lib():
                                       ctypes.c_int, ctypes.c_int, ip, ctypes.c_float,
                                       ctypes.c_float, dp, dp, dp]
             L.orc_amp_tau.restype = None
+            L.orc_tau_ref_f32.argtypes = [fp, fp, ctypes.c_int, fp, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ip, ctypes.c_float, ctypes.c_float, fp, fp]
+            L.orc_tau_ref_f32.restype = None
             L.orc_ism_sum.argtypes = [dp, dp, ctypes.c_long, ctypes.c_long, ctypes.c_int,
                                       ctypes.c_float, dp, ctypes.c_long]
             L.orc_ism_sum.restype = None
@@ -132,6 +135,21 @@ def amp_tau(room_sz, beta, pos_src, pos_rcv, nb_img, fs, spkr_pattern="omni",
                       _p(nb, ctypes.c_int), float(np.float32(c)), float(np.float32(fs)),
                       _p(amp, ctypes.c_double), _p(tau, ctypes.c_double), _p(tdp, ctypes.c_double))
     return amp, tau, tdp
+
+
+def tau_reference_f32(room_sz, pos_src, pos_rcv, nb_img, fs, spkr_pattern="omni", mic_pattern="omni",
+                      c=343.0):
+    """Image delays rounded in float32 as the reference build forms them (the
+    engine's reference-delay mode): tau [M_src, M_rcv, N], tau_dp [M_src, M_rcv]."""
+    room, _, ps, pr, _, _, nb = _geometry_args(room_sz, np.zeros(6), pos_src, pos_rcv, None, None, nb_img)
+    ms, mr, N = ps.shape[0], pr.shape[0], int(np.prod(nb))
+    tau = np.zeros((ms, mr, N), dtype=np.float32)
+    tdp = np.zeros((ms, mr), dtype=np.float32)
+    lib().orc_tau_ref_f32(_p(room, ctypes.c_float), _p(ps, ctypes.c_float), ms, _p(pr, ctypes.c_float), mr,
+                          PATTERNS[spkr_pattern], PATTERNS[mic_pattern], _p(nb, ctypes.c_int),
+                          float(np.float32(c)), float(np.float32(fs)), _p(tau, ctypes.c_float),
+                          _p(tdp, ctypes.c_float))
+    return tau, tdp
 
 
 def ism_sum(amp, tau, n_ism, fs, ld=None):

@@ -27,8 +27,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(_HERE, "_ref")
 CUBIN = os.path.join(REF_DIR, "gpuRIR_ref.cubin")
-# The reference checkout; the recipe below reads src/gpuRIR_cuda.cu there.
-REF_ROOT = os.environ.get("GPURIR_REFERENCE_ROOT", "/root/reference")
+# The reference checkout (given to build_ref, or by GPURIR_REFERENCE_ROOT); the
+# recipe below reads src/gpuRIR_cuda.cu there.
+REF_ROOT = os.environ.get("GPURIR_REFERENCE_ROOT")
 
 # Itanium-mangled names of the reference kernels (signatures at
 # src/gpuRIR_cuda.cu:245, 377, 392, 415, 445, 492, 515, 541, 559).
@@ -55,10 +56,12 @@ _LUT_OVERSAMP = 16
 def build_ref(root=None, force=False):
     """Compile the reference's device code into oracle/_ref/gpuRIR_ref.cubin.
 
-    Returns the cubin path, or None when the reference checkout is absent
-    (the cubin built earlier, if any, is then used as is)."""
-    src = os.path.join(root or REF_ROOT, "src", "gpuRIR_cuda.cu")
-    if not os.path.exists(src):
+    `root` is the reference checkout (default: $GPURIR_REFERENCE_ROOT).  Returns
+    the cubin path, or None when the checkout is absent (the cubin built
+    earlier, if any, is then used as is)."""
+    root = root or REF_ROOT
+    src = os.path.join(root, "src", "gpuRIR_cuda.cu") if root else ""
+    if not src or not os.path.exists(src):
         return CUBIN if os.path.exists(CUBIN) else None
     if not force and os.path.exists(CUBIN) and os.path.getmtime(CUBIN) >= os.path.getmtime(src):
         return CUBIN

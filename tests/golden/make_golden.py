@@ -2,7 +2,7 @@
 
 Run in the build container, where the reference checkout exists:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the gpuRIR checkout>
 
 gpuRIR/__init__.py imports a compiled module ``gpuRIR_bind`` whose constructor
 needs a GPU; a stub module stands in for it here.  The stub only records the
@@ -149,4 +149,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the gpuRIR checkout>")
+    main(sys.argv[1])

@@ -59,11 +59,17 @@ def test_lut_mode_matches_gpuRIR_lut_semantics(built, fs):
 def test_mode_flags_exclude_each_other(built):
     import gpurir_gb300 as G
     sim = G.Simulator()
-    assert sim.modes() == dict(mixed_precision=False, lut=False)
+    assert sim.modes() == dict(mixed_precision=False, lut=False, reference_delays=False)
     sim.activate_lut(True)
     sim.activate_mixed_precision(True)
-    assert sim.modes() == dict(mixed_precision=True, lut=False)
+    assert sim.modes() == dict(mixed_precision=True, lut=False, reference_delays=False)
     sim.activate_lut(True)
-    assert sim.modes() == dict(mixed_precision=False, lut=True)
+    assert sim.modes() == dict(mixed_precision=False, lut=True, reference_delays=False)
     sim.activate_lut(False)
-    assert sim.modes() == dict(mixed_precision=False, lut=False)
+    assert sim.modes() == dict(mixed_precision=False, lut=False, reference_delays=False)
+    # the delay model is independent of the evaluation mode
+    sim.activate_reference_delays(True)
+    sim.activate_mixed_precision(True)
+    assert sim.modes() == dict(mixed_precision=True, lut=False, reference_delays=True)
+    sim.activate_reference_delays(False)
+    assert sim.modes() == dict(mixed_precision=True, lut=False, reference_delays=False)

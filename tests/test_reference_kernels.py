@@ -13,9 +13,12 @@ remaining difference of the full pipeline is the reference's float32 delay
 (dist / c * Fs in single precision, up to ~4e-4 samples off at 0.3 s), which
 the oracle and the engine compute more accurately.
 
-GPU tests compare the engine with the same outputs, and (when
-oracle/_ref/gpuRIR_ref.cubin is present) with the reference's kernels run live
-on random scenes.
+The engine's reference-delay mode rounds each delay in float32 as the
+reference's kernel does (bit for bit, pinned here on every scene); with it the
+engine matches the reference's FP32 and LUT outputs within 1e-5 relative L2 and
+its half2 output within 2e-3.  GPU tests compare the engine with the same
+outputs, and (when oracle/_ref/gpuRIR_ref.cubin is present) with the
+reference's kernels run live on random scenes.
 """
 import json
 import os
@@ -147,12 +150,46 @@ def test_oracle_pipeline_vs_reference_kernels(name):
     assert rel_l2(out["fp32/early"].reshape(got.shape), got) < 2e-4
 
 
+def _tau_ref(sc):
+    return oracle.tau_reference_f32(sc["room_sz"], sc["pos_src"], sc["pos_rcv"], sc["nb_img"], sc["fs"],
+                                    INV[sc["spkr_pattern"]], INV[sc["mic_pattern"]])
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_oracle_reference_delays_bit_exact(name):
+    """The float32 delay model (the engine's reference-delay mode) reproduces
+    every delay and direct-path delay calcAmpTau_kernel wrote, bit for bit."""
+    sc, out = SCENES[name]
+    tau, tdp = _tau_ref(sc)
+    assert np.array_equal(tau, out["tau"].reshape(tau.shape))
+    assert np.array_equal(tdp, out["tau_dp"].reshape(tdp.shape))
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_oracle_with_reference_delays_matches_reference(name):
+    """FP64 amplitudes with the float32 delays: the whole early part agrees
+    with the reference's FP32 and LUT outputs to float32 rounding, and with its
+    half2 path to the error of its half-precision accumulation."""
+    sc, out = SCENES[name]
+    amp, _, _ = _amp_tau(sc)
+    tau, _ = _tau_ref(sc)
+    n = oracle.n_samples(sc["Tdiff"], sc["fs"])
+    got = oracle.ism_sum(amp, tau.astype(np.float64), n, sc["fs"])
+    assert rel_l2(out["fp32/early"].reshape(got.shape), got) < 1e-6
+    if "lut" in sc["modes"]:
+        lut = oracle.ism_sum_lut(amp, tau.astype(np.float64), n, sc["fs"])
+        assert rel_l2(out["lut/early"].reshape(lut.shape), lut) < 5e-7
+    if "mp" in sc["modes"]:
+        assert rel_l2(out["mp/early"].reshape(got.shape), got) < 2e-3
+
+
 # ---------------------------------------------------------------------------------- GPU
 
 
-def _engine(sc, mode="fp32"):
+def _engine(sc, mode="fp32", reference_delays=False):
     import gpurir_gb300 as G
-    sim = G.Simulator(seed=1, mixed_precision=(mode == "mp"), lut=(mode == "lut"))
+    sim = G.Simulator(seed=1, mixed_precision=(mode == "mp"), lut=(mode == "lut"),
+                      reference_delays=reference_delays)
     r = sim.simulate_rir(sc["room_sz"], sc["beta"], sc["pos_src"], sc["pos_rcv"], sc["orV_src"],
                          sc["orV_rcv"], sc["spkr_pattern"], sc["mic_pattern"], sc["nb_img"], sc["Tdiff"],
                          sc["Tmax"], sc["fs"])
@@ -161,11 +198,39 @@ def _engine(sc, mode="fp32"):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(SCENES))
+def test_engine_reference_delays_match_reference_kernels(built, name):
+    """Reference-delay mode against gpuRIR's own kernels: FP32 and LUT within
+    1e-5 relative L2, mixed precision within 2e-3 (the reference accumulates
+    in half precision), and each mode within float32 rounding of the oracle
+    fed the same delays."""
+    sc, out = SCENES[name]
+    n = oracle.n_samples(sc["Tdiff"], sc["fs"])
+    amp, _, _ = _amp_tau(sc)
+    tau, _ = _tau_ref(sc)
+    for mode in sc["modes"]:
+        _, r = _engine(sc, mode, reference_delays=True)
+        ref = out["%s/early" % mode]
+        e_ref = rel_l2(r[..., :n], ref)
+        if mode == "lut":
+            want = oracle.ism_sum_lut(amp, tau.astype(np.float64), n, sc["fs"]).reshape(ref.shape)
+        else:
+            want = oracle.ism_sum(amp, tau.astype(np.float64), n, sc["fs"]).reshape(ref.shape)
+        e_orc = rel_l2(r[..., :n], want)
+        print("%s %s: vs reference %.2e, vs oracle %.2e" % (name, mode, e_ref, e_orc))
+        assert e_ref < (2e-3 if mode == "mp" else 1e-5)
+        assert e_orc < (5e-4 if mode == "mp" else 1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(SCENES))
 def test_engine_matches_reference_kernels(built, name):
+    """Default (exact-delay) mode against the reference: bounded by the
+    reference's float32 delays, and closer to the exact sum than it."""
     sc, out = SCENES[name]
     n = oracle.n_samples(sc["Tdiff"], sc["fs"])
     sim, r = _engine(sc)
     ref = out["fp32/early"]
+    print("%s: default mode vs reference %.2e" % (name, rel_l2(r[..., :n], ref)))
     assert rel_l2(r[..., :n], ref) < 2e-4
     amp, tau, _ = _amp_tau(sc)
     exact = oracle.ism_sum(amp, tau, n, sc["fs"]).reshape(ref.shape)
@@ -208,6 +273,20 @@ def test_engine_envelope_matches_reference_kernels(built):
     assert np.all(np.abs(env[:, 2] - rtd) <= 1e-6 * rtd)
 
 
+@pytest.mark.gpu
+def test_engine_envelope_reference_delays(built):
+    """With reference delays the direct-path delay is the reference's bit for
+    bit, and A follows its early part to float32 rounding."""
+    sc, out = SCENES["tail"]
+    sim, r = _engine(sc, reference_delays=True)
+    env = sim.last_envelope(r.shape[0] * r.shape[1])
+    assert np.array_equal(env[:, 2], out["tau_dp"].ravel())
+    rA = out["A"].ravel().astype(np.float64)
+    assert np.all(np.abs(env[:, 0] - rA) <= 1e-5 * np.abs(rA) + 1e-30)
+    ral = out["alpha"].ravel().astype(np.float64)
+    assert np.all(np.abs(env[:, 1] - ral) <= 1e-6 * np.abs(ral))
+
+
 def _random_scene(rng):
     fs = float(rng.choice([8000.0, 16000.0, 22050.0, 44100.0, 48000.0]))
     room = rng.uniform([3, 3, 2.5], [9, 7, 4]).astype(np.float32)
@@ -245,4 +324,17 @@ def test_live_reference_kernels_random_scenes(built):
         assert rel_l2(lut["early"], fed_lut) < 5e-7
         _, r = _engine(sc)
         assert rel_l2(r[..., :n], ref["early"]) < 3e-4
+        # the float32 delay model is the reference's, bit for bit, on every pattern pair
+        inv = {v: k for k, v in oracle.PATTERNS.items()}
+        tau, tdp = oracle.tau_reference_f32(sc["room_sz"], sc["pos_src"], sc["pos_rcv"], sc["nb_img"],
+                                            sc["fs"], inv[sc["spkr_pattern"]], inv[sc["mic_pattern"]])
+        assert np.array_equal(tau, ref["tau"].reshape(tau.shape))
+        assert np.array_equal(tdp, ref["tau_dp"].reshape(tdp.shape))
+        _, rr = _engine(sc, reference_delays=True)
+        assert rel_l2(rr[..., :n], ref["early"]) < 1e-5
+        _, rl = _engine(sc, "lut", reference_delays=True)
+        assert rel_l2(rl[..., :n], lut["early"]) < 1e-5
+        mp = rk.simulate(mode="mp", **kw)
+        _, rm = _engine(sc, "mp", reference_delays=True)
+        assert rel_l2(rm[..., :n], mp["early"]) < 2e-3
     rk.close()

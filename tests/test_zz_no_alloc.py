@@ -93,3 +93,33 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(built):
         16000.0, 343.0, out.data_ptr(), None)
     assert rc == -1
     assert b"8192" in L.gpurir_last_error()
+
+
+def test_noalloc_limit_counts_segments_of_long_rirs(built):
+    """The 8192-item scratch holds RIRs x segments: at 16 kHz a 2 s RIR is cut
+    into 7 segments of at most 5120 samples, so 1170 RIRs fit and 1600 do not
+    (rejected on the host before anything is enqueued)."""
+    import torch
+    from gpurir_gb300 import _lib
+    L = _lib.load()
+    dev = torch.device("cuda")
+    room = np.array([6.0, 5.0, 3.0], np.float32)
+    beta = np.full(6, 0.8, np.float32)
+    nb = np.array([3, 3, 3], np.int32)
+    n = L.gpurir_n_samples(2.0, 16000.0)
+    for ns, nr, ok in ((39, 30, True), (40, 40, False)):
+        rng = np.random.default_rng(ns)
+        ps = torch.from_numpy((0.5 + rng.random((ns, 3)) * (room - 1.0)).astype(np.float32)).to(dev)
+        pr = torch.from_numpy((0.5 + rng.random((nr, 3)) * (room - 1.0)).astype(np.float32)).to(dev)
+        out = torch.full((ns, nr, n) if ok else (1,), float("nan"), device=dev)
+        rc = L.gpurir_simulate_ism_noalloc(
+            room.ctypes.data_as(_lib.fptr), beta.ctypes.data_as(_lib.fptr), ps.data_ptr(), ns, pr.data_ptr(),
+            None, None, 0, 0, nr, nb.ctypes.data_as(_lib.iptr), 2.0, 16000.0, 343.0, out.data_ptr(),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        if ok:
+            assert rc == 0, L.gpurir_last_error()
+            assert bool(torch.isfinite(out).all())
+        else:
+            assert rc == -1
+            assert b"segments" in L.gpurir_last_error()
