@@ -116,15 +116,49 @@ class ClockSampler:
 
 
 def _cpu_port_sample(scene, n_src, threads):
-    """RIRs/s of the FP32 CPU restatement of the early part on `n_src` sources."""
+    """(RIRs, windowed updates, seconds) of the FP32 CPU restatement of the whole
+    per-RIR work (early part, envelope, diffuse tail: every sample of every RIR)
+    on the first `n_src` sources and all receivers."""
     import oracle
     t = time.perf_counter()
-    out, upd = oracle.ism_f32(scene["room_sz"], scene["beta"], scene["pos_src"][:n_src],
-                              scene["pos_rcv"], scene["nb_img"], scene["Tdiff"], scene["fs"],
-                              scene["spkr_pattern"], scene["mic_pattern"], None,
-                              scene["orV_rcv"], scene["c"], n_threads=threads)
+    out, upd = oracle.rir_f32(scene["room_sz"], scene["beta"], scene["pos_src"][:n_src],
+                              scene["pos_rcv"], scene["nb_img"], scene["Tmax"], scene["fs"],
+                              scene["Tdiff"], scene["spkr_pattern"], scene["mic_pattern"], None,
+                              scene["orV_rcv"], scene["c"], noise=scene["noise"], n_threads=threads)
     dt = time.perf_counter() - t
     return n_src * scene["pos_rcv"].shape[0], upd, dt
+
+
+def _accuracy(G, scene, d_out, seed, offset):
+    """Max-abs and relative-L2 error of an output of the mic_array workload against
+    the FP64 oracle, on 64 RIRs spread over the sources and receivers (every 8th
+    source x every 4th receiver), early part and tail separately."""
+    import oracle
+    ms, mr = scene["pos_src"].shape[0], scene["pos_rcv"].shape[0]
+    src_i, rcv_i = np.arange(0, ms, 8), np.arange(0, mr, 4)
+    got = d_out[src_i][:, rcv_i].cpu().numpy().astype(np.float64)
+    want = np.zeros_like(got)
+    n_ism = None
+    for a, s_idx in enumerate(src_i):
+        ref, parts = oracle.simulate_rir(
+            scene["room_sz"], scene["beta"], scene["pos_src"][s_idx:s_idx + 1], scene["pos_rcv"][rcv_i],
+            scene["nb_img"], scene["Tmax"], scene["fs"], scene["Tdiff"], scene["spkr_pattern"],
+            scene["mic_pattern"], None, scene["orV_rcv"][rcv_i], scene["c"], seed=seed, offset=offset,
+            noise=scene["noise"], return_parts=True, rir_index=s_idx * mr + rcv_i)
+        want[a] = ref[0]
+        n_ism = parts["n_ism"]
+
+    def stats(x, y):
+        n = float(np.linalg.norm(y))
+        return {"rel_l2": float(np.linalg.norm(x - y)) / n if n > 0 else None,
+                "max_abs": float(np.abs(x - y).max()), "ref_max_abs": float(np.abs(y).max())}
+
+    return {"vs": "fp64 oracle (oracle/ism_oracle.c)", "rirs_checked": int(got.shape[0] * got.shape[1]),
+            "which": "timed output of the last step: sources 0,8,..,56 x receivers 0,4,..,28",
+            "early": stats(got[..., :n_ism], want[..., :n_ism]),
+            "tail": stats(got[..., n_ism:], want[..., n_ism:]),
+            "note": "the tail of this workload is silent: its images end before the 10 ms envelope "
+                    "window at Tdiff (nb_img [12,14,24] reaches ~0.18 s), so A = 0 in both"}
 
 
 def run_reference(a):
@@ -135,7 +169,7 @@ def run_reference(a):
     scene = workloads.mic_array()
     threads = os.cpu_count() or 1
     n_src = 4
-    for _ in range(max(a.warmup, 1)):
+    for _ in range(min(max(a.warmup, 1), 3)):
         _cpu_port_sample(scene, n_src, threads)
     times, n_rir, upd = [], 0, 0
     for _ in range(a.steps):
@@ -143,7 +177,8 @@ def run_reference(a):
         times.append(dt)
     step_s = sum(times) / len(times)
     value = n_rir / step_s
-    sample = "%d of 64 sources x 32 receivers (%d RIRs) per step, early part only" % (n_src, n_rir)
+    sample = ("%d of 64 sources x 32 receivers (%d RIRs) per step, every sample of each RIR (early "
+              "part, envelope, diffuse tail): the same per-RIR work as the GPU arm" % (n_src, n_rir))
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "RIRs/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -153,9 +188,11 @@ def run_reference(a):
                              "sample": sample},
             "e2e": {"value": value, "unit": "RIRs/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
+            "same_config": True,
             "note": "runs on the host cores: the reference has no CPU implementation of the path, "
-                    "so its FP32 restatement (OpenMP, windowed) is timed; gpuRIR's own CUDA kernels "
-                    "on the same GPU are timed by oracle/time_reference_kernels.py"}
+                    "so its FP32 restatement (OpenMP, windowed, early part + envelope + tail) is "
+                    "timed; gpuRIR's own CUDA kernels on the same GPU are timed by "
+                    "oracle/time_reference_kernels.py"}
     print(json.dumps(line), flush=True)
 
 
@@ -401,6 +438,10 @@ def run_gpu(a):
         torch.distributed.barrier()
         total_ms = max_over_ranks(total_ms)
     clk = clocks.stop()
+    # accuracy of the timed output (outside the timed region): the last step drew the
+    # tail of call counter calls - 1
+    seed_used, calls_after = sim.get_seed()
+    accuracy = _accuracy(G, scene, d_out, seed_used, calls_after - 1) if rank == 0 else None
     ms_per_step = total_ms / a.steps
     value = world * M * a.steps / (total_ms * 1e-3)
 
@@ -478,7 +519,7 @@ def run_gpu(a):
                     "kernel_ms": e2e_kernel_ms / a.steps,
                     "d2h": "kernel stores into the pinned host buffer over NVLink-C2C" if direct
                            else "cudaMemcpyAsync after the kernels"},
-            "roofline": roofline, "clocks": clk, "gpu_launches": launches}
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches, "accuracy": accuracy}
     if world == 1 and not a.no_extras:
         line["workloads"] = run_extras(G, flush, stream, tuple(a.extras.split(",")))
     if world == 1 and not a.no_cpu_baseline:
@@ -487,8 +528,8 @@ def run_gpu(a):
         n_rir, upd, dt = _cpu_port_sample(scene_cpu, 16, threads)
         line["cpu_baseline"] = {"value": n_rir / dt, "unit": "RIRs/s", "cores": threads,
                                 "kind": "port", "updates_per_s": upd / dt,
-                                "sample": "16 of 64 sources x 32 receivers (%d RIRs), early part, "
-                                          "FP32 OpenMP restatement" % n_rir}
+                                "sample": "16 of 64 sources x 32 receivers (%d RIRs), every sample "
+                                          "(early part, envelope, tail), FP32 OpenMP restatement" % n_rir}
     print(json.dumps(line), flush=True)
 
 

@@ -52,12 +52,13 @@ def mic_array():
 
 
 def batched_rooms(n_rooms=512, c=343.0):
-    from . import beta_sabine_closed_form
+    from . import beta_SabineEstimation
     rng = np.random.default_rng(2)
     dims = np.stack([rng.uniform(3, 10, n_rooms), rng.uniform(3, 8, n_rooms),
                      rng.uniform(2.5, 4.5, n_rooms)], axis=1)
     t60 = rng.uniform(0.2, 1.2, n_rooms)
-    betas = beta_sabine_closed_form(dims, t60)
+    # beta per room by the reference's own estimator (scipy L-BFGS-B, gpuRIR/__init__.py:22-54)
+    betas = [beta_SabineEstimation(dims[i], t60[i]) for i in range(n_rooms)]
     rooms = []
     for i in range(n_rooms):
         tdiff = 0.4 * t60[i]

@@ -450,19 +450,80 @@ static float orc_directivity_f(const float doa[3], const float orv[3], int patte
     }
 }
 
-/* rir : [M_src*M_rcv][ld] floats, columns [0, nISM) written.  Returns the
- * number of windowed image-sample updates performed. */
-long long orc_ism_f32(const float room[3], const float beta[6],
+/* 1 when every axis index is the central one (the direct path, clust = refl = 0). */
+static int cl_all_zero(const int n[3], const int N[3])
+{
+    return n[0] == N[0] / 2 && n[1] == N[1] / 2 && n[2] == N[2] / 2;
+}
+
+/* Envelope and diffuse tail of one RIR in float32, as envPred_kernel and
+ * diffRev_kernel compute them per RIR and per sample (src/gpuRIR_cuda.cu:415-461):
+ * mean power of the last <= 10 ms after the direct path, A and alpha from the
+ * Sabine T60, then noise times sqrtf(A * expf(alpha * (nISM + s - tau_dp))).  The
+ * noise comes from the Philox stream of this engine (the reference draws cuRAND
+ * uniforms): logistic (noise_kind 0) or Gaussian. */
+static void orc_tail_f32(float *h, int nISM, int nDiff, float tau_dp, float Fs, float T60,
+                         uint64_t seed, uint64_t offset, uint32_t rir, int noise_kind)
+{
+    const float w_sz = 10e-3f * Fs;
+    float lo = (float)nISM - w_sz;
+    if (tau_dp > lo) lo = tau_dp;
+    const int ws = (int)ceilf(lo);
+    const float alpha = -13.8155f / (T60 * Fs);
+    float A = 0.0f;
+    if (ws < nISM) {
+        const float wc = (float)ws + (float)(nISM - ws) / 2.0f;
+        float p = 0.0f;
+        for (int t = ws; t < nISM; t++) p += h[t] * h[t];
+        p /= (float)(nISM - ws);
+        A = p / expf(alpha * (wc - tau_dp));
+    }
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int s0 = 0; s0 < nDiff; s0 += 4) {
+        const uint32_t ctr[4] = {(uint32_t)(s0 >> 2), rir, (uint32_t)offset, (uint32_t)(offset >> 32)};
+        uint32_t w[4];
+        orc_philox4x32_10(ctr, key, w);
+        float z[4];
+        if (noise_kind == 0) {
+            for (int q = 0; q < 4; q++) {
+                const float u = ((float)(w[q] >> 9) + 0.5f) * 1.1920928955078125e-07f;
+                z[q] = 0.551329f * logf(u / (1.0f - u + 1e-6f));
+            }
+        } else {
+            for (int q = 0; q < 4; q += 2) {
+                const float u1 = ((float)(w[q] >> 9) + 0.5f) * 1.1920928955078125e-07f;
+                const float u2 = ((float)(w[q + 1] >> 9) + 0.5f) * 1.1920928955078125e-07f;
+                const float r = sqrtf(-2.0f * logf(u1));
+                z[q] = r * cosf(6.283185307f * u2);
+                z[q + 1] = r * sinf(6.283185307f * u2);
+            }
+        }
+        for (int q = 0; q < 4 && s0 + q < nDiff; q++) {
+            const float env = A * expf(alpha * ((float)(nISM + s0 + q) - tau_dp));
+            h[nISM + s0 + q] = sqrtf(env) * z[q];
+        }
+    }
+}
+
+/* rir : [M_src*M_rcv][ld] floats, columns [0, nTotal) written: the early part
+ * [0, nISM) and, when nTotal > nISM, the envelope-shaped tail (the reference's
+ * whole per-RIR work).  Returns the number of windowed image-sample updates. */
+long long orc_rir_f32(const float room[3], const float beta[6],
                       const float *pos_src, int M_src, const float *pos_rcv, int M_rcv,
                       const float *orv_src, const float *orv_rcv, int spkr_pattern, int mic_pattern,
-                      const int nb_img[3], float c, float Fs, int nISM, float *rir, long ld,
-                      int n_threads)
+                      const int nb_img[3], float c, float Fs, int nISM, int nTotal, uint64_t seed,
+                      uint64_t offset, int noise_kind, float *rir, long ld, int n_threads)
 {
     const int N0 = nb_img[0], N1 = nb_img[1], N2 = nb_img[2];
     const float PIf = 3.141592654f;
     const float Tw = (float)orc_window_len(Fs);
     const float H = Tw / 2.0f;
     const long M = (long)M_src * M_rcv;
+    /* SabineT60 in float32 as the reference's device function evaluates it (:123-130) */
+    const float Sa = ((1.0f - beta[0] * beta[0]) + (1.0f - beta[1] * beta[1])) * room[1] * room[2] +
+                     ((1.0f - beta[2] * beta[2]) + (1.0f - beta[3] * beta[3])) * room[0] * room[2] +
+                     ((1.0f - beta[4] * beta[4]) + (1.0f - beta[5] * beta[5])) * room[0] * room[1];
+    const float T60f = 0.161f * (room[0] * room[1] * room[2]) / Sa;
     long long updates = 0;
 #ifdef _OPENMP
     if (n_threads > 0) omp_set_num_threads(n_threads);
@@ -472,6 +533,7 @@ long long orc_ism_f32(const float room[3], const float beta[6],
         int ms = (int)(m / M_rcv), mr = (int)(m % M_rcv);
         float *h = rir + m * ld;
         for (int t = 0; t < nISM; t++) h[t] = 0.0f;
+        float tau_dp = 0.0f;
         for (int n0 = 0; n0 < N0; n0++)
         for (int n1 = 0; n1 < N1; n1++)
         for (int n2 = 0; n2 < N2; n2++) {
@@ -491,6 +553,7 @@ long long orc_ism_f32(const float room[3], const float beta[6],
             if (spkr_pattern != P_OMNI) a *= orc_directivity_f(im2rcv, osrc, spkr_pattern);
             if (mic_pattern != P_OMNI) a *= orc_directivity_f(vec, &orv_rcv[mr * 3], mic_pattern);
             float ta = dist / c * Fs;
+            if (cl_all_zero(n, N)) tau_dp = ta;
             long t0 = (long)floorf(ta - H);
             if (t0 < 0) t0 = 0;
             for (long t = t0; t < nISM && (float)t < ta + H; t++) {
@@ -503,6 +566,19 @@ long long orc_ism_f32(const float room[3], const float beta[6],
                 updates++;
             }
         }
+        if (nTotal > nISM) orc_tail_f32(h, nISM, nTotal - nISM, tau_dp, Fs, T60f, seed, offset,
+                                        (uint32_t)m, noise_kind);
     }
     return updates;
+}
+
+/* The early part only. */
+long long orc_ism_f32(const float room[3], const float beta[6],
+                      const float *pos_src, int M_src, const float *pos_rcv, int M_rcv,
+                      const float *orv_src, const float *orv_rcv, int spkr_pattern, int mic_pattern,
+                      const int nb_img[3], float c, float Fs, int nISM, float *rir, long ld,
+                      int n_threads)
+{
+    return orc_rir_f32(room, beta, pos_src, M_src, pos_rcv, M_rcv, orv_src, orv_rcv, spkr_pattern,
+                       mic_pattern, nb_img, c, Fs, nISM, nISM, 0, 0, 0, rir, ld, n_threads);
 }

@@ -85,6 +85,11 @@ def lib():
                                       ctypes.c_float, ctypes.c_int, fp, ctypes.c_long,
                                       ctypes.c_int]
             L.orc_ism_f32.restype = ctypes.c_longlong
+            L.orc_rir_f32.argtypes = [fp, fp, fp, ctypes.c_int, fp, ctypes.c_int, fp, fp,
+                                      ctypes.c_int, ctypes.c_int, ip, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                      ctypes.c_int, fp, ctypes.c_long, ctypes.c_int]
+            L.orc_rir_f32.restype = ctypes.c_longlong
             _lib = L
     return _lib
 
@@ -239,7 +244,7 @@ NOISE_KINDS = {"logistic": 0, "gaussian": 1}
 
 def simulate_rir(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
                  spkr_pattern="omni", mic_pattern="omni", orV_src=None, orV_rcv=None, c=343.0,
-                 seed=1234, offset=0, noise="logistic", return_parts=False, rir_base=0):
+                 seed=1234, offset=0, noise="logistic", return_parts=False, rir_base=0, rir_index=None):
     """FP64 restatement of cuda_simulateRIR (src/gpuRIR_cuda.cu:766-931).
 
     Returns float64 [M_src, M_rcv, nSamples]: the early part by the ISM, the rest
@@ -256,7 +261,10 @@ def simulate_rir(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None,
     out = ism_sum(amp.reshape(ms * mr, -1), tau.reshape(ms * mr, -1), n_ism, fs, ld=n_tot)
     A, al = env_pred(out, tdp, n_ism, fs, room_sz, beta)
     if n_diff > 0:
-        idx = np.arange(rir_base, rir_base + ms * mr, dtype=np.uint32)   # Philox stream per RIR
+        # Philox stream per RIR: its global index in the call (C order [src][rcv] from rir_base,
+        # or given per RIR when the pairs are a subset of a larger call)
+        idx = (np.arange(rir_base, rir_base + ms * mr, dtype=np.uint32) if rir_index is None else
+               np.ascontiguousarray(np.asarray(rir_index, dtype=np.uint32).reshape(ms * mr)))
         lib().orc_tail(_p(A, ctypes.c_double), _p(al, ctypes.c_double),
                        _p(np.ascontiguousarray(tdp.reshape(-1)), ctypes.c_double), ms * mr,
                        n_ism, n_diff, int(seed), int(offset), _p(idx, ctypes.c_uint32),
@@ -286,6 +294,29 @@ def ism_f32(room_sz, beta, pos_src, pos_rcv, nb_img, Tdiff, fs, spkr_pattern="om
                             PATTERNS[spkr_pattern], PATTERNS[mic_pattern], _p(nb, ctypes.c_int),
                             float(np.float32(c)), float(np.float32(fs)), n_ism,
                             _p(out, ctypes.c_float), n_ism, int(n_threads))
+    return out, int(upd)
+
+
+def rir_f32(room_sz, beta, pos_src, pos_rcv, nb_img, Tmax, fs, Tdiff=None, spkr_pattern="omni",
+            mic_pattern="omni", orV_src=None, orV_rcv=None, c=343.0, seed=1234, offset=0, noise="logistic",
+            n_threads=0):
+    """FP32 threaded CPU port of the whole per-RIR work of the reference (early part,
+    envelope, diffuse tail): the timed CPU baseline.
+
+    Returns (rir float32 [M_src, M_rcv, nSamples], windowed updates performed).
+    """
+    room, b, ps, pr, os_, or_, nb = _geometry_args(room_sz, beta, pos_src, pos_rcv,
+                                                   orV_src, orV_rcv, nb_img)
+    Tdiff = Tmax if Tdiff is None else Tdiff
+    n_ism, n_tot = n_samples(Tdiff, fs), n_samples(Tmax, fs)
+    ms, mr = ps.shape[0], pr.shape[0]
+    out = np.zeros((ms, mr, n_tot), dtype=np.float32)
+    upd = lib().orc_rir_f32(_p(room, ctypes.c_float), _p(b, ctypes.c_float),
+                            _p(ps, ctypes.c_float), ms, _p(pr, ctypes.c_float), mr,
+                            _p(os_, ctypes.c_float), _p(or_, ctypes.c_float),
+                            PATTERNS[spkr_pattern], PATTERNS[mic_pattern], _p(nb, ctypes.c_int),
+                            float(np.float32(c)), float(np.float32(fs)), n_ism, n_tot, int(seed), int(offset),
+                            NOISE_KINDS[noise], _p(out, ctypes.c_float), n_tot, int(n_threads))
     return out, int(upd)
 
 
