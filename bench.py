@@ -377,6 +377,33 @@ def _extra_trajectory(workloads, sim, flush, stream, fs, dev):
                          "conv_hbm_gbs": conv_bytes / (t_conv * 1e-3) / 1e9,
                          "note": "400 points x 8 mics, 12800-sample RIRs, 10 s signal; segments "
                                  "uploaded from host memory inside the timed call"}
+    # forward + adjoint: RIRs from the differentiable batch (beta on the device), the filtered
+    # signal, an L2 loss against a target, gradients w.r.t. the signal and beta
+    from gpurir_gb300.autograd import TorchBatch
+    from gpurir_gb300.trajectory import simulate_trajectory_torch
+    model = TorchBatch([dict(tr, spkr_pattern="omni", mic_pattern="omni")], fs, sim=sim)
+    beta = torch.tensor(np.asarray(tr["beta"], np.float32), device=dev).reshape(1, 6).requires_grad_(True)
+    sig = torch.from_numpy(tr["signal"]).to(dev).requires_grad_(True)
+    with torch.no_grad():
+        target = simulate_trajectory_torch(sig, model(beta * 0.99, tps, tpr).view(400, 8, 12800), sim=sim)
+
+    def t_fwd():
+        with torch.no_grad():
+            simulate_trajectory_torch(sig, model(beta, tps, tpr).view(400, 8, 12800), sim=sim)
+
+    def t_fwd_bwd():
+        y = simulate_trajectory_torch(sig, model(beta, tps, tpr).view(400, 8, 12800), sim=sim)
+        ((y - target) ** 2).sum().backward()
+
+    for _ in range(3):
+        t_fwd(); t_fwd_bwd()
+    tf = _timed(t_fwd, 10, stream, flush)
+    tfb = _timed(t_fwd_bwd, 10, stream, flush)
+    out["trajectory"].update({"forward_ms": tf, "forward_adjoint_ms": tfb, "adjoint_over_forward": tfb / tf,
+                              "adjoint_note": "RIRs (early part + tail) and the filtered signal; then "
+                                              "dL/dsignal [160000] and dL/dbeta [6] of an L2 loss, through "
+                                              "the trajectory adjoint (FFT correlations) and the "
+                                              "image-source adjoint"})
     return out
 
 

@@ -83,6 +83,8 @@ SIGNATURES.update({
                                          c_void_p, c_void_p]),
     "gpurir_trajectory": (c_int, [c_void_p, c_void_p, c_int, c_int, iptr, c_void_p, c_int, c_int,
                                   c_void_p]),
+    "gpurir_trajectory_adjoint_device": (c_int, [c_void_p, c_void_p, c_int, c_int, iptr, c_void_p, c_int,
+                                                 c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "gpurir_simulate_ism_noalloc": (c_int, [fptr, fptr, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
                                             c_int, c_int, c_int, iptr, c_float, c_float, c_float,
                                             c_void_p, c_void_p]),

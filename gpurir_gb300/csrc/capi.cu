@@ -59,6 +59,10 @@ cudaError_t rir_conv_launch(const float *rir, int P, int R, int L, int S, int M,
                             cudaStream_t st);
 cudaError_t ola_launch(const float *conv, long conv_ld, const int *w_ini, const int *w_len, int P, int R,
                        int L, long n_out, int uni_w, double *out, cudaStream_t st);
+int traj_adjoint_grid(int M, int P, int num_sms);
+cudaError_t traj_adjoint_launch(const double *g, long n_out, const int *w_ini, const int *w_len, const float *rir,
+                                int P, int R, int L, int M, const float2 *W, const float2 *Sg, float *gt,
+                                float *grad_rir, float *grad_sig, float2 *acc, int grid, cudaStream_t st);
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
 cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
                                   int n_items, const float *pos_src, const float *pos_rcv, unsigned char *skip,
@@ -1533,6 +1537,48 @@ extern "C" int gpurir_trajectory_device(gpurir_sim *s, const float *d_segments, 
     if (!s || !d_segments || !w_ini || !d_rir || !d_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
     return trajectory_core(s, d_segments, n_pts, seg_len, w_ini, d_rir, n_rcv, rir_len, d_out, nullptr,
                            nullptr, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gpurir_trajectory_adjoint_device(gpurir_sim *s, const float *d_segments, int n_pts, int seg_len,
+                                                const int *w_ini, const float *d_rir, int n_rcv, int rir_len,
+                                                const double *d_grad_out, float *d_grad_signal,
+                                                float *d_grad_rir, void *stream) {
+    if (!s || !d_segments || !w_ini || !d_rir || !d_grad_out) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if (n_pts < 1 || n_rcv < 1 || seg_len < 1 || rir_len < 1) return fail(GPURIR_ERR_INVALID, "empty trajectory");
+    std::vector<int> win;
+    int rc = check_windows(w_ini, n_pts, seg_len, win);
+    if (rc) return rc;
+    if (!d_grad_signal && !d_grad_rir) return GPURIR_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const long n = (long)seg_len + rir_len - 1;
+    if (n > 16384) return fail(GPURIR_ERR_UNSUPPORTED, "trajectory adjoint: segment + RIR longer than 16384 samples");
+    // the register FFT kernels cover N = 2048 .. 16384: shorter problems are zero-padded to 2048
+    const int N = std::max(fft_size(n), 2048), M = N / 2;
+    const long n_out = (long)w_ini[n_pts] + rir_len - 1;
+    const int grid = traj_adjoint_grid(M, n_pts, s->num_sms);
+    if (s->conv_recorded) CK(cudaStreamWaitEvent(st, s->conv_busy, 0));
+    const size_t o_sg = 0;
+    const size_t o_gt = align_up(o_sg + (size_t)n_pts * (M + 1) * sizeof(float2), 256);
+    const size_t o_acc = align_up(o_gt + (size_t)n_rcv * n_out * sizeof(float), 256);
+    const size_t o_win = align_up(o_acc + (size_t)grid * (M + 1) * sizeof(float2), 256);
+    const size_t bytes = align_up(o_win + win.size() * sizeof(int), 256);
+    if ((rc = ensure_conv(s, bytes))) return rc;
+    const float2 *W = nullptr;
+    if ((rc = get_twiddles(s, N, st, &W))) return rc;
+    if ((rc = ensure_stage(s, win.size() * sizeof(int)))) return rc;
+    memcpy(s->h_stage, win.data(), win.size() * sizeof(int));
+    int *dwin = reinterpret_cast<int *>(s->d_conv + o_win);
+    CK(cudaMemcpyAsync(dwin, s->h_stage, win.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(s->stage_done, st));
+    s->stage_pending = true;
+    float2 *Sg = reinterpret_cast<float2 *>(s->d_conv + o_sg);
+    CK(segment_spectra_launch(d_segments, n_pts, seg_len, M, W, Sg, nullptr, s->num_sms, st));
+    CK(traj_adjoint_launch(d_grad_out, n_out, dwin, dwin + n_pts + 1, d_rir, n_pts, n_rcv, rir_len, M, W, Sg,
+                           reinterpret_cast<float *>(s->d_conv + o_gt), d_grad_rir, d_grad_signal,
+                           reinterpret_cast<float2 *>(s->d_conv + o_acc), grid, st));
+    CK(cudaEventRecord(s->conv_busy, st));
+    s->conv_recorded = true;
+    return GPURIR_OK;
 }
 
 extern "C" int gpurir_trajectory(gpurir_sim *s, const float *segments, int n_pts, int seg_len,

@@ -653,6 +653,181 @@ static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S,
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of simulateTrajectory (no counterpart in the reference, which is not
+// differentiable).  The forward pass is, per point p and receiver r,
+//   y[w_ini[p] + j][r] += (x_p * h_pr)[j],  0 <= j < w_len[p] + L - 1,
+// with x_p the segment of point p and h_pr its RIR.  Given g = dL/dy:
+//   dL/dh_pr[k] = sum_t g_pr[t + k] x_p[t]             (correlation with the segment)
+//   dL/dx_p[t]  = sum_r sum_k g_pr[t + k] h_pr[k]       (correlation with the RIRs)
+// where g_pr[j] = g[w_ini[p] + j][r] on the window the forward pass wrote.  Both
+// are computed as spectra: D = G conj(X) and sum_r G conj(H), with the real FFTs
+// of the forward kernel (N = 2M >= S + L - 1, so no circular wrap on the kept
+// lags).  One block per point walks its receivers: FFT of the gradient window and
+// of the RIR, the product with the segment's spectrum inverted to dL/dh, the
+// product with the RIR's spectrum added to the point's accumulator (bins owned by
+// one thread each: no atomics), and at the end the accumulator inverted to dL/dx.
+// ---------------------------------------------------------------------------
+
+// g [n_out][R] float64 -> gt [R][n_out] float32 (rows the FFT kernels read contiguously)
+__global__ void grad_transpose_kernel(const double *__restrict__ g, long n_out, int R, float *__restrict__ gt) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_out) return;
+    for (int r = 0; r < R; r++) gt[(long)r * n_out + t] = (float)g[t * R + r];
+}
+
+// Real-spectrum bins k and M - k of the packed FFT z (natural order in buf).
+__device__ __forceinline__ void real_bins(const float2 *buf, int k, int M, float2 wk, float2 &xk, float2 &xm) {
+    const int km = (M - k) & (M - 1);
+    const float2 zk = buf[pad16(k)], zm = buf[pad16(km)];
+    const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+    const float2 wm = make_float2(-wk.x, wk.y);
+    xk = cadd(ze, cmul(wk, zo));
+    xm = cadd(ze2, cmul(wm, zo2));
+}
+
+// Packs the real spectrum (bins k, M - k) into buf for the inverse packed FFT.
+__device__ __forceinline__ void pack_inverse(float2 *buf, int k, int M, float2 wk, float2 yk, float2 ym) {
+    const int km = (M - k) & (M - 1);
+    const float2 wm = make_float2(-wk.x, wk.y);
+    const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
+    const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
+    buf[pad16(k)] = make_float2(yec.x - yod.y, yec.y + yod.x);
+    if (k != 0 && km != k) {
+        const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
+        const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
+        buf[pad16(km)] = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+    }
+}
+
+// Stores the first n values of the inverse packed FFT in buf (z[n] = y[2n] + i y[2n+1]).
+template <int M>
+__device__ __forceinline__ void store_real(const float2 *buf, float *__restrict__ o, int n) {
+    constexpr int T = M / 16;
+    if ((reinterpret_cast<uintptr_t>(o) & 7) == 0) {
+        for (int c = threadIdx.x; 2 * c < n; c += T) {
+            const float2 z = buf[pad16(c)];
+            if (2 * c + 1 < n) reinterpret_cast<float2 *>(o)[c] = z;
+            else o[2 * c] = z.x;
+        }
+    } else {
+        for (int i = threadIdx.x; i < n; i += T) {
+            const float2 z = buf[pad16(i >> 1)];
+            o[i] = (i & 1) ? z.y : z.x;
+        }
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(M / 16) traj_adjoint_kernel(
+        const float *__restrict__ gt, long n_out, const int *__restrict__ w_ini, const int *__restrict__ w_len,
+        const float *__restrict__ rir, int P, int R, int L, const float2 *__restrict__ W,
+        const float2 *__restrict__ Sg, float *__restrict__ grad_rir, float *__restrict__ grad_sig,
+        float2 *__restrict__ acc_all) {
+    constexpr int T = M / 16, BS = M + M / 16;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *bg = sm, *bh = sm + BS;   // gradient window, RIR
+    const int j = threadIdx.x;
+    float2 *acc = acc_all + (size_t)blockIdx.x * (M + 1);
+    const float inv_m = 1.0f / (float)M;
+    float2 v[16];
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        const int w0 = w_ini[p], wl = w_len[p];
+        const int glen = wl + L - 1;   // gradient entries the forward pass wrote for this point
+        const float2 *xs = Sg + (size_t)p * (M + 1);   // segment spectrum / M
+        for (int r = 0; r < R; r++) {
+            load_packed<M>(gt + (size_t)r * n_out + w0, glen, v);
+            reg_fft<false, M, true>(v, bg, W);
+            if (grad_sig) {
+                load_packed<M>(rir + ((size_t)p * R + r) * L, L, v);
+                reg_fft<false, M, true>(v, bh, W);
+            }
+            for (int k = j; k <= M / 2; k += T) {
+                const float2 wk = __ldg(&W[k]);
+                float2 gk, gm;
+                real_bins(bg, k, M, wk, gk, gm);
+                if (grad_sig) {
+                    float2 hk, hm;
+                    real_bins(bh, k, M, wk, hk, hm);
+                    float2 ak = cmul(gk, cconj(hk)), am = cmul(gm, cconj(hm));
+                    if (r > 0) {
+                        ak = cadd(ak, acc[k]);
+                        am = cadd(am, acc[M - k]);
+                    }
+                    acc[k] = ak;
+                    if (M - k != k) acc[M - k] = am;
+                }
+                if (grad_rir) {
+                    const float2 dk = cmul(gk, cconj(__ldg(&xs[k])));
+                    const float2 dm = cmul(gm, cconj(__ldg(&xs[M - k])));
+                    pack_inverse(bg, k, M, wk, dk, dm);   // (k, M - k) of this thread only
+                }
+            }
+            __syncthreads();
+            if (grad_rir) {
+                reg_fft<true, M, false>(v, bg, W);
+                store_real<M>(bg, grad_rir + ((size_t)p * R + r) * L, L);
+                __syncthreads();
+            }
+        }
+        if (grad_sig) {
+            for (int k = j; k <= M / 2; k += T) {   // the bins this thread accumulated
+                const float2 wk = __ldg(&W[k]);
+                const float2 ak = acc[k], am = acc[M - k];
+                pack_inverse(bg, k, M, wk, make_float2(ak.x * inv_m, ak.y * inv_m),
+                             make_float2(am.x * inv_m, am.y * inv_m));
+            }
+            __syncthreads();
+            reg_fft<true, M, false>(v, bg, W);
+            store_real<M>(bg, grad_sig + w0, wl);
+            __syncthreads();
+        }
+    }
+}
+
+template <int M>
+static cudaError_t launch_traj_adjoint(const float *gt, long n_out, const int *w_ini, const int *w_len,
+                                       const float *rir, int P, int R, int L, const float2 *W,
+                                       const float2 *Sg, float *grad_rir, float *grad_sig, float2 *acc,
+                                       int grid, cudaStream_t st) {
+    const size_t smem = (size_t)2 * (M + M / 16) * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(traj_adjoint_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    traj_adjoint_kernel<M><<<grid, M / 16, smem, st>>>(gt, n_out, w_ini, w_len, rir, P, R, L, W, Sg, grad_rir,
+                                                       grad_sig, acc);
+    return cudaGetLastError();
+}
+
+// Blocks of the adjoint kernel for FFT half-size M (one per SM at most: the kernel
+// holds two padded rows of shared memory).
+int traj_adjoint_grid(int M, int P, int num_sms) {
+    (void)M;
+    return std::max(1, std::min(P, num_sms * (M <= 4096 ? 2 : 1)));
+}
+
+cudaError_t traj_adjoint_launch(const double *g, long n_out, const int *w_ini, const int *w_len, const float *rir,
+                                int P, int R, int L, int M, const float2 *W, const float2 *Sg, float *gt,
+                                float *grad_rir, float *grad_sig, float2 *acc, int grid, cudaStream_t st) {
+    if (n_out <= 0 || P <= 0 || R <= 0) return cudaSuccess;
+    grad_transpose_kernel<<<(unsigned)((n_out + 255) / 256), 256, 0, st>>>(g, n_out, R, gt);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    switch (M) {
+    case 1024: return launch_traj_adjoint<1024>(gt, n_out, w_ini, w_len, rir, P, R, L, W, Sg, grad_rir, grad_sig, acc, grid, st);
+    case 2048: return launch_traj_adjoint<2048>(gt, n_out, w_ini, w_len, rir, P, R, L, W, Sg, grad_rir, grad_sig, acc, grid, st);
+    case 4096: return launch_traj_adjoint<4096>(gt, n_out, w_ini, w_len, rir, P, R, L, W, Sg, grad_rir, grad_sig, acc, grid, st);
+    case 8192: return launch_traj_adjoint<8192>(gt, n_out, w_ini, w_len, rir, P, R, L, W, Sg, grad_rir, grad_sig, acc, grid, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 // Overlap-add (gpuRIR/__init__.py:216-219): out[t][r] = sum over points p, in
 // increasing p, of conv[p][r][t - w_ini[p]] for 0 <= t - w_ini[p] < w_len[p] + L - 1.
 // Compensated FP32 sum (two-sum), written as float64.

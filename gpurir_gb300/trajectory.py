@@ -80,3 +80,93 @@ def simulate_trajectory(source_signal, RIRs, timestamps=None, fs=None, sim=None)
                                    w.ctypes.data_as(_lib.iptr), rir.ctypes.data, R, Lr,
                                    out.ctypes.data), "gpurir_trajectory")
     return out
+
+
+class _Trajectory:
+    """torch.autograd.Function of simulateTrajectory on device tensors (built lazily:
+    importing this module does not import torch)."""
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            import torch
+
+            class Fn(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, signal, rirs, w_ini, seg_len, sim):
+                    from . import _lib
+                    import ctypes
+                    dseg = _segments_device(signal, w_ini, seg_len)
+                    P, R, Lr = rirs.shape
+                    out = torch.empty((int(w_ini[-1]) + Lr - 1, R), dtype=torch.float64, device=rirs.device)
+                    st = torch.cuda.current_stream(rirs.device).cuda_stream
+                    _lib.check(_lib.load().gpurir_trajectory_device(
+                        sim.handle, dseg.data_ptr(), P, seg_len, w_ini.ctypes.data_as(_lib.iptr), rirs.data_ptr(),
+                        R, Lr, out.data_ptr(), ctypes.c_void_p(st)), "gpurir_trajectory_device")
+                    ctx.save_for_backward(dseg, rirs)
+                    ctx.w_ini, ctx.seg_len, ctx.sim, ctx.n_sig = w_ini, seg_len, sim, signal.shape[0]
+                    return out
+
+                @staticmethod
+                def backward(ctx, grad_out):
+                    from . import _lib
+                    import ctypes
+                    dseg, rirs = ctx.saved_tensors
+                    P, R, Lr = rirs.shape
+                    g = grad_out.to(torch.float64).contiguous()
+                    gs = torch.zeros(ctx.n_sig, dtype=torch.float32, device=rirs.device) \
+                        if ctx.needs_input_grad[0] else None
+                    gr = torch.empty_like(rirs) if ctx.needs_input_grad[1] else None
+                    st = torch.cuda.current_stream(rirs.device).cuda_stream
+                    _lib.check(_lib.load().gpurir_trajectory_adjoint_device(
+                        ctx.sim.handle, dseg.data_ptr(), P, ctx.seg_len, ctx.w_ini.ctypes.data_as(_lib.iptr),
+                        rirs.data_ptr(), R, Lr, g.data_ptr(), gs.data_ptr() if gs is not None else None,
+                        gr.data_ptr() if gr is not None else None, ctypes.c_void_p(st)),
+                        "gpurir_trajectory_adjoint_device")
+                    return gs, gr, None, None, None
+
+            cls.fn = Fn
+        return cls.fn
+
+
+def _segments_device(signal, w_ini, seg_len):
+    """Segments [n_pts, seg_len] of a device signal (zero-padded), as segment_signal cuts them."""
+    import torch
+    n_pts = len(w_ini) - 1
+    w_len = np.diff(w_ini)
+    if np.all(w_len == seg_len) and np.array_equal(w_ini[:-1], seg_len * np.arange(n_pts)):
+        return signal[:n_pts * seg_len].reshape(n_pts, seg_len).contiguous()
+    # one gather: destination (p, t) <- signal[w_ini[p] + t] for t < w_len[p]
+    t = np.arange(seg_len)
+    keep = t[None, :] < w_len[:, None]
+    dst = np.nonzero(keep.ravel())[0]
+    src = (w_ini[:-1, None] + t[None, :]).ravel()[dst]
+    seg = torch.zeros(n_pts * seg_len, dtype=torch.float32, device=signal.device)
+    seg[torch.from_numpy(dst).to(signal.device)] = signal[torch.from_numpy(src).to(signal.device)]
+    return seg.view(n_pts, seg_len)
+
+
+def simulate_trajectory_torch(source_signal, RIRs, timestamps=None, fs=None, sim=None):
+    """simulateTrajectory on float32 CUDA tensors with autograd: returns the float64
+    [len(signal) + L - 1, R] tensor; its backward gives dL/dsignal and dL/dRIRs
+    (FFT correlations on the device, gpurir_trajectory_adjoint_device).  Chain RIRs
+    from gpurir_gb300.autograd to reach the wall coefficients and positions."""
+    import torch
+    from . import simulator
+    sim = sim or simulator()
+    if not (source_signal.is_cuda and RIRs.is_cuda):
+        raise ValueError("source_signal and RIRs must be CUDA tensors")
+    sig = source_signal.to(torch.float32).contiguous()
+    rirs = RIRs.to(torch.float32).contiguous()
+    n_pts = rirs.shape[0]
+    n = sig.shape[0]
+    assert timestamps is None or fs is not None, "fs must be indicated for custom timestamps"
+    if timestamps is None:
+        w_ini = np.append((np.arange(n_pts) * (n / n_pts)).astype(int), n)
+    else:
+        assert timestamps[0] == 0, "The first timestamp must be 0"
+        w_ini = np.append((np.asarray(timestamps) * fs).astype(int), n)
+    w_ini = np.ascontiguousarray(w_ini.astype(np.int32))
+    seg_len = int(np.diff(w_ini).max())
+    return _Trajectory.get().apply(sig, rirs, w_ini, seg_len, sim)

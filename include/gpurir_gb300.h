@@ -237,6 +237,21 @@ int gpurir_trajectory_device(gpurir_sim *sim, const float *d_segments, int n_pts
 int gpurir_trajectory(gpurir_sim *sim, const float *segments, int n_pts, int seg_len, const int *w_ini,
                       const float *rir, int n_rcv, int rir_len, double *out);
 
+/* Adjoint of gpurir_trajectory_device (same segments, windows and RIRs): given
+ * d_grad_out = dL/dout, float64 [w_ini[n_pts] + rir_len - 1][n_rcv], writes
+ *   d_grad_signal  float32 [w_ini[n_pts]]: dL/dsignal (sample w_ini[p] + t is
+ *                  sample t of segment p), and
+ *   d_grad_rir     float32 [n_pts][n_rcv][rir_len]: dL/dRIR,
+ * either may be NULL.  FFT correlations with the segment's spectrum (dL/dRIR)
+ * and with the RIRs' spectra summed over receivers (dL/dsignal), FP32, for
+ * seg_len + rir_len - 1 <= 16384.  Device buffers, stream-ordered.  gpuRIR's
+ * simulateTrajectory (gpuRIR/__init__.py:177-221) is not differentiable; this
+ * has no counterpart there. */
+int gpurir_trajectory_adjoint_device(gpurir_sim *sim, const float *d_segments, int n_pts, int seg_len,
+                                     const int *w_ini, const float *d_rir, int n_rcv, int rir_len,
+                                     const double *d_grad_out, float *d_grad_signal, float *d_grad_rir,
+                                     void *stream);
+
 /* Early part of one room's RIRs without allocating any memory.  No counterpart
  * in the reference.  For callers that must not call cudaMalloc while they run:
  * real-time audio threads (cudaMalloc may block on a device synchronisation),

@@ -347,3 +347,29 @@ def trajectory(source_signal, RIRs, timestamps=None, fs=None):
             y = np.convolve(seg, np.asarray(RIRs[p, r], dtype=np.float64))
             out[w_ini[p]:w_ini[p] + len(y), r] += y
     return out
+
+
+def trajectory_adjoint(source_signal, RIRs, grad_out, timestamps=None, fs=None):
+    """FP64 adjoint of `trajectory` (the engine's gpurir_trajectory_adjoint_device):
+    given dL/dout [n + L - 1, R], returns (dL/dsignal [n], dL/dRIRs [P, R, L]) by
+    direct correlations: dL/dh_pr[k] = sum_t g[w_ini[p] + t + k, r] x_p[t] and
+    dL/dx_p[t] = sum_r sum_k g[w_ini[p] + t + k, r] h_pr[k]."""
+    sig = np.asarray(source_signal)
+    n = len(sig)
+    P, R, L = RIRs.shape
+    if timestamps is None:
+        fs = n / P
+        timestamps = np.arange(P)
+    w_ini = np.append((np.asarray(timestamps) * fs).astype(int), n)
+    g = np.asarray(grad_out, dtype=np.float64)
+    gsig = np.zeros(n)
+    grir = np.zeros((P, R, L))
+    for p in range(P):
+        a, b = w_ini[p], w_ini[p + 1]
+        seg = np.asarray(sig[a:b], dtype=np.float32).astype(np.float64)
+        win = g[a:b + L - 1]                       # the rows the forward pass wrote for this point
+        for r in range(R):
+            h = np.asarray(RIRs[p, r], dtype=np.float64)
+            grir[p, r] = np.correlate(win[:, r], seg, mode="valid")[:L] if len(seg) else 0.0
+            gsig[a:b] += np.correlate(win[:, r], h, mode="valid")
+    return gsig, grir

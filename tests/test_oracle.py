@@ -208,3 +208,22 @@ def test_torch_fp64_reference_matches_oracle():
     ref = oracle.simulate_rir(room, beta, ps, pr, [5, 6, 7], 0.06, 16000.0, spkr_pattern="card",
                               mic_pattern="bidir", orV_src=os_, orV_rcv=or_)
     assert np.abs(h - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("timestamps,fs", [(None, None), ([0.0, 0.7, 1.9, 3.2], 20.0)])
+def test_trajectory_adjoint_is_the_transpose(timestamps, fs):
+    """The FP64 adjoint of the trajectory filter satisfies <G, J v> = <J^T G, v>
+    for perturbations of the signal and of the RIRs (the filter is bilinear)."""
+    rng = np.random.default_rng(3)
+    P, R, L, n = 4, 3, 37, 103
+    sig = rng.standard_normal(n).astype(np.float32)
+    h = rng.standard_normal((P, R, L)).astype(np.float32)
+    y = oracle.trajectory(sig, h, timestamps, fs)
+    G = rng.standard_normal(y.shape)
+    gs, gr = oracle.trajectory_adjoint(sig, h, G, timestamps, fs)
+    ds = rng.standard_normal(n).astype(np.float32)
+    dh = rng.standard_normal((P, R, L)).astype(np.float32)
+    lhs_s = np.sum(G * oracle.trajectory(ds, h, timestamps, fs))
+    lhs_h = np.sum(G * oracle.trajectory(sig, dh, timestamps, fs))
+    assert abs(lhs_s - np.dot(gs, ds)) <= 1e-10 * max(1.0, abs(lhs_s))
+    assert abs(lhs_h - np.sum(gr * dh)) <= 1e-10 * max(1.0, abs(lhs_h))
