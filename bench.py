@@ -347,10 +347,20 @@ def _extra_inverse(workloads, sim, flush, stream, fs, dev):
         fwd_bwd()
     t_gf = _timed(g_f.replay, 20, stream, flush)
     t_gfb = _timed(g_fb.replay, 20, stream, flush)
+
+    # the same step through the fused L2 entry: forward, loss, its gradient and the adjoint
+    # in one C call that writes the parameters' .grad (no autograd graph)
+    def fused_step():
+        model.l2_step(beta, ps, pr, None, orv, target)
+
+    for _ in range(3):
+        fused_step()
+    t_fused = _timed(fused_step, 20, stream, flush)
     out["inverse_problem"] = {"rirs": 16 * 32, "forward_ms": t_f, "forward_adjoint_ms": t_fb,
                               "adjoint_over_forward": t_fb / t_f,
                               "graph_forward_ms": t_gf, "graph_forward_adjoint_ms": t_gfb,
                               "graph_adjoint_over_forward": t_gfb / t_gf,
+                              "fused_l2_step_ms": t_fused, "fused_l2_step_over_forward": t_fused / t_f,
                               "note": "grads of an L2 loss w.r.t. beta[16,6], pos_src[64,3], "
                                       "pos_rcv[128,3]; beta stays on the device (TorchBatch)"}
     return out

@@ -95,6 +95,7 @@ SIGNATURES.update({
     "gpurir_adjoint_forward": (c_int, [c_void_p] * 8),
     "gpurir_adjoint_backward": (c_int, [c_void_p] * 13),
     "gpurir_adjoint_status": (c_int, [c_void_p, iptr]),
+    "gpurir_adjoint_l2_step": (c_int, [c_void_p] * 7 + [c_float] + [c_void_p] * 8),
     "gpurir_adjoint_destroy": (c_int, [c_void_p]),
     "gpurir_simulate_batch_device_beta": (c_int, [c_void_p, c_int, ctypes.POINTER(Room), c_float, c_float]
                                           + [c_void_p] * 7),

@@ -64,6 +64,37 @@ class _IsmBatch(torch.autograd.Function):
         return gb, gs, gr, gos, gor, None
 
 
+class _L2Step(torch.autograd.Function):
+    """loss = scale * sum (RIRs - target)^2 with its gradients computed in the same
+    fused call (gpurir_adjoint_l2_step); backward only scales them by dL/dloss."""
+
+    @staticmethod
+    def forward(ctx, beta, pos_src, pos_rcv, orV_src, orV_rcv, target, batch, scale):
+        dev = pos_src.device
+        out = torch.empty(batch.total, dtype=torch.float32, device=dev)
+        loss = torch.empty((), dtype=torch.float32, device=dev)
+        need = ctx.needs_input_grad
+        gb = torch.empty((batch.n_rooms, 6), dtype=torch.float32, device=dev) if need[0] else None
+        gs = torch.empty_like(pos_src) if need[1] else None
+        gr = torch.empty_like(pos_rcv) if need[2] else None
+        gos = torch.empty_like(orV_src) if orV_src is not None and need[3] else None
+        gor = torch.empty_like(orV_rcv) if orV_rcv is not None and need[4] else None
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        st = torch.cuda.current_stream(dev).cuda_stream
+        _lib.check(_lib.load().gpurir_adjoint_l2_step(
+            batch.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
+            target.data_ptr(), float(scale), out.data_ptr(), loss.data_ptr(), ptr(gb), ptr(gs), ptr(gr),
+            ptr(gos), ptr(gor), ctypes.c_void_p(st)), "gpurir_adjoint_l2_step")
+        batch._forwards += 1
+        batch.last_rirs = out
+        ctx.grads = (gb, gs, gr, gos, gor)
+        return loss
+
+    @staticmethod
+    def backward(ctx, grad_loss):
+        return tuple(None if g is None else g * grad_loss for g in ctx.grads) + (None, None, None)
+
+
 class TorchBatch:
     """The static structure of a batch (room sizes, image counts, lengths, patterns,
     per-room source/receiver counts) prepared once on the device (gpurir_adjoint);
@@ -106,6 +137,61 @@ class TorchBatch:
         contig = lambda t: t.contiguous() if t is not None else None
         return _IsmBatch.apply(beta.reshape(self.n_rooms, 6).contiguous(), contig(pos_src), contig(pos_rcv),
                                contig(orV_src), contig(orV_rcv), self)
+
+
+    def l2_loss(self, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, target=None, reduction="sum"):
+        """The L2 loss of the packed RIRs against `target` (float32 CUDA tensor of the
+        packed size), reduction "sum" or "mean", as a scalar tensor with autograd.
+        Forward, loss, its gradient and the adjoint run in one fused call
+        (gpurir_adjoint_l2_step); loss.backward() only scales the gradients it
+        computed.  The RIRs of the call are left in ``self.last_rirs``."""
+        for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv, target):
+            if t is not None and (t.dtype != torch.float32 or not t.is_cuda):
+                raise ValueError("beta, positions, orientations and target must be float32 CUDA tensors")
+        if target is None or target.numel() != self.total:
+            raise ValueError("target must hold the batch's packed RIRs (%d values)" % self.total)
+        scale = 1.0 if reduction == "sum" else 1.0 / self.total
+        contig = lambda t: t.contiguous() if t is not None else None
+        return _L2Step.apply(beta.reshape(self.n_rooms, 6).contiguous(), contig(pos_src), contig(pos_rcv),
+                             contig(orV_src), contig(orV_rcv), target.reshape(-1).contiguous(), self, scale)
+
+    def l2_step(self, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, target=None, reduction="sum"):
+        """One fused training step without the autograd graph: forward, the L2 loss
+        against `target`, its gradient and the adjoint in one C call
+        (gpurir_adjoint_l2_step).  The gradient of every input that requires grad
+        is written into its ``.grad`` (allocated on the first call, overwritten on
+        later ones: no zero_grad needed); returns the loss as a 0-d tensor.  The
+        RIRs of the step are left in ``self.last_rirs``.  Nothing waits for the GPU:
+        the host only enqueues kernels, so an optimizer step can follow at once."""
+        if target is None or target.numel() != self.total:
+            raise ValueError("target must hold the batch's packed RIRs (%d values)" % self.total)
+        for t in (beta, pos_src, pos_rcv, orV_src, orV_rcv, target):
+            if t is not None and (t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous()):
+                raise ValueError("beta, positions, orientations and target must be contiguous float32 CUDA "
+                                 "tensors")
+        dev = pos_src.device
+        if getattr(self, "_l2_bufs", None) is None or self._l2_bufs[0].device != dev:
+            self._l2_bufs = (torch.empty(self.total, dtype=torch.float32, device=dev),
+                             torch.empty((), dtype=torch.float32, device=dev))
+        out, loss = self._l2_bufs
+
+        def grad_of(t):
+            if t is None or not t.requires_grad:
+                return None
+            if t.grad is None or t.grad.shape != t.shape:
+                t.grad = torch.empty_like(t)
+            return t.grad.data_ptr()
+
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        scale = 1.0 if reduction == "sum" else 1.0 / self.total
+        _lib.check(self._L.gpurir_adjoint_l2_step(
+            self.handle, beta.data_ptr(), ptr(pos_src), ptr(pos_rcv), ptr(orV_src), ptr(orV_rcv),
+            target.data_ptr(), scale, out.data_ptr(), loss.data_ptr(), grad_of(beta), grad_of(pos_src),
+            grad_of(pos_rcv), grad_of(orV_src), grad_of(orV_rcv),
+            ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), "gpurir_adjoint_l2_step")
+        self._forwards += 1
+        self.last_rirs = out
+        return loss
 
 
 def simulate_batch_torch(rooms, fs, beta, pos_src, pos_rcv, orV_src=None, orV_rcv=None, c=343.0,

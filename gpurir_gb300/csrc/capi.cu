@@ -64,6 +64,9 @@ cudaError_t traj_adjoint_launch(const double *g, long n_out, const int *w_ini, c
                                 int P, int R, int L, int M, const float2 *W, const float2 *Sg, float *gt,
                                 float *grad_rir, float *grad_sig, float2 *acc, int grid, cudaStream_t st);
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
+int l2_grad_blocks(long n);
+cudaError_t l2_grad_launch(const float *y, const float *t, long n, float scale, float *g, double *partial,
+                           float *loss, cudaStream_t st);
 cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
                                   int n_items, const float *pos_src, const float *pos_rcv, unsigned char *skip,
                                   cudaStream_t st);
@@ -1227,11 +1230,16 @@ struct gpurir_adjoint {
     bool need_orv_src = false, need_orv_rcv = false;
     bool rooms_written = false;   // a forward call has written the room tables
     size_t o_arr[6] = {}, o_ig = 0, o_ctl = 0;
+    float *d_g = nullptr;         // dL/dRIR of the fused L2 step (allocated by its first call)
+    double *d_partial = nullptr;  // per-block partial sums of the loss
 };
 
 extern "C" int gpurir_adjoint_destroy(gpurir_adjoint *a) {
     if (!a) return GPURIR_OK;
+    if (a->d_g || a->d_partial) cudaDeviceSynchronize();
     if (a->d) cudaFree(a->d);
+    if (a->d_g) cudaFree(a->d_g);
+    if (a->d_partial) cudaFree(a->d_partial);
     delete a;
     return GPURIR_OK;
 }
@@ -1348,6 +1356,27 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
     float *const outs[5] = {d_grad_beta, d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src, d_grad_orV_rcv};
     CK(grad_reduce_launch(ig, dp, a->n_rooms, (int)a->ns, (int)a->nr, outs, st));
     return GPURIR_OK;
+}
+
+extern "C" int gpurir_adjoint_l2_step(gpurir_adjoint *a, const float *d_beta, const float *d_pos_src,
+                                      const float *d_pos_rcv, const float *d_orV_src, const float *d_orV_rcv,
+                                      const float *d_target, float scale, float *d_out, float *d_loss,
+                                      float *d_grad_beta, float *d_grad_pos_src, float *d_grad_pos_rcv,
+                                      float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream) {
+    if (!a || !d_target || !d_out || !d_loss) return fail(GPURIR_ERR_INVALID, "NULL argument");
+    if ((reinterpret_cast<uintptr_t>(d_target) | reinterpret_cast<uintptr_t>(d_out)) & 15)
+        return fail(GPURIR_ERR_INVALID, "d_target and d_out must be 16-byte aligned");
+    if (!a->d_g) {   // first call: the gradient buffer and the loss partials
+        CK(cudaMalloc(&a->d_g, sizeof(float) * std::max<long long>(a->out_elems, 4)));
+        CK(cudaMalloc(&a->d_partial, sizeof(double) * 1024));
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int rc = gpurir_adjoint_forward(a, d_beta, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_out, stream);
+    if (rc) return rc;
+    CK(l2_grad_launch(d_out, d_target, (long)a->out_elems, scale, a->d_g, a->d_partial, d_loss, st));
+    // the room tables of the forward just enqueued serve the adjoint (same beta)
+    return gpurir_adjoint_backward(a, nullptr, d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, a->d_g, d_grad_beta,
+                                   d_grad_pos_src, d_grad_pos_rcv, d_grad_orV_src, d_grad_orV_rcv, stream);
 }
 
 extern "C" int gpurir_adjoint_status(gpurir_adjoint *a, int *status) {

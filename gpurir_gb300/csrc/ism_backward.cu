@@ -402,12 +402,10 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
 #undef acc
 }
 
-// Sum of item partials per target: one warp per target of the five sets (rooms:
-// beta; sources: position, orientation; receivers: position, orientation).  Target t
-// of a set sums components [comp_lo, comp_lo + n_comp) of the items list[ptr[t]..
-// ptr[t+1]) into out[t * n_comp + c]: lane l takes list entries l, l + 32, ... in
-// order, then the lanes are added by a fixed xor tree, so the result does not depend
-// on timing.  A set with out == nullptr has no targets.
+// Sum of item partials per target of the five sets (rooms: beta; sources: position,
+// orientation; receivers: position, orientation).  Target t of a set sums components
+// [comp_lo, comp_lo + n_comp) of the items list[ptr[t]..ptr[t+1]) into
+// out[t * n_comp + c].  A set with out == nullptr has no targets.
 struct GradSet {
     const int *ptr, *list;
     int n_target, comp_lo, n_comp;
@@ -417,14 +415,21 @@ struct GradSets {
     GradSet s[5];
 };
 
-__global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    int t = gw, k = 0;
+// One block per target: its threads take the target's items in a fixed stride, then
+// a fixed xor tree per warp and the warp sums in order -- deterministic, and a target
+// with thousands of items (one room of a long trajectory) is summed by the whole
+// block instead of one warp.
+constexpr int kRedThreads = 128;
+
+__global__ void __launch_bounds__(kRedThreads) grad_reduce_kernel(const float *item_grad, GradSets G) {
+    __shared__ float red[kRedThreads / 32][6];
+    int t = blockIdx.x, k = 0;
     while (k < 5 && t >= G.s[k].n_target) t -= G.s[k++].n_target;
     if (k == 5) return;
     const GradSet S = G.s[k];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int p = S.ptr[t] + lane; p < S.ptr[t + 1]; p += 32) {
+    for (int p = S.ptr[t] + threadIdx.x; p < S.ptr[t + 1]; p += kRedThreads) {
         const float *row = item_grad + (long)S.list[p] * kGrad + S.comp_lo;
 #pragma unroll
         for (int c = 0; c < 6; c++)
@@ -434,7 +439,14 @@ __global__ void grad_reduce_kernel(const float *item_grad, GradSets G) {
     for (int c = 0; c < 6; c++) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
-        if (lane == 0 && c < S.n_comp) S.out[t * S.n_comp + c] = v[c];
+        if (lane == 0) red[warp][c] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < S.n_comp) {
+        float sum = 0.0f;
+#pragma unroll
+        for (int w = 0; w < kRedThreads / 32; w++) sum += red[w][threadIdx.x];
+        S.out[t * S.n_comp + threadIdx.x] = sum;
     }
 }
 
@@ -499,13 +511,14 @@ cudaError_t grad_reduce_launch(const float *item_grad, const int *const csr[6], 
     GradSets G;
     const int n_t[5] = {n_rooms, n_src, n_rcv, n_src, n_rcv};
     const int which[5] = {0, 1, 2, 1, 2}, lo[5] = {0, 6, 9, 12, 15}, nc[5] = {6, 3, 3, 3, 3};
-    long warps = 0;
+    long targets = 0;
     for (int k = 0; k < 5; k++) {
         G.s[k] = GradSet{csr[2 * which[k]], csr[2 * which[k] + 1], out[k] ? n_t[k] : 0, lo[k], nc[k], out[k]};
-        warps += G.s[k].n_target;
+        targets += G.s[k].n_target;
     }
-    if (warps <= 0) return cudaSuccess;
-    grad_reduce_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(item_grad, G);
+    if (targets <= 0) return cudaSuccess;
+    if (targets > 0x7fffffffL) return cudaErrorInvalidValue;
+    grad_reduce_kernel<<<(unsigned)targets, kRedThreads, 0, st>>>(item_grad, G);
     return cudaGetLastError();
 }
 

@@ -208,6 +208,21 @@ int gpurir_adjoint_backward(gpurir_adjoint *adj, const float *d_beta, const floa
                             float *d_grad_pos_rcv, float *d_grad_orV_src, float *d_grad_orV_rcv,
                             void *stream);
 int gpurir_adjoint_status(gpurir_adjoint *adj, int *status);
+
+/* One fused training step of the L2 fit of a batch to target RIRs: the forward
+ * pass into d_out (packed layout), loss = scale * sum (d_out - d_target)^2 into
+ * d_loss (one float on the device) and, in the same pass over the samples, the
+ * gradient 2 scale (d_out - d_target) that the adjoint then consumes; the
+ * gradients are written as by gpurir_adjoint_backward (each may be NULL).  The
+ * loss is summed in a fixed order (bitwise reproducible).  Enqueues kernels only,
+ * except that the first call on `adj` allocates its gradient buffer
+ * (out_elems floats): make it before any stream capture.  d_target and d_out
+ * 16-byte aligned.  Used for the inverse problem; no counterpart in the reference. */
+int gpurir_adjoint_l2_step(gpurir_adjoint *adj, const float *d_beta, const float *d_pos_src,
+                           const float *d_pos_rcv, const float *d_orV_src, const float *d_orV_rcv,
+                           const float *d_target, float scale, float *d_out, float *d_loss,
+                           float *d_grad_beta, float *d_grad_pos_src, float *d_grad_pos_rcv,
+                           float *d_grad_orV_src, float *d_grad_orV_rcv, void *stream);
 int gpurir_adjoint_destroy(gpurir_adjoint *adj);
 
 /* Batched FFT convolutions of trajectory segments with their RIRs, host
