@@ -202,6 +202,10 @@ void orc_ism_sum(const double *amp, const double *tau, long M, long N, int nISM,
 {
     const double Tw = (double)orc_window_len(Fs);
     const double H = Tw / 2.0;
+    /* RIRs in parallel; each RIR's sum runs in image order on one thread */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
     for (long m = 0; m < M; m++) {
         double *h = rir + m * ld;
         for (int t = 0; t < nISM; t++) h[t] = 0.0;
@@ -272,6 +276,9 @@ void orc_ism_sum_lut(const double *amp, const double *tau, long M, long N, int n
     float *T = (float *)malloc(sizeof(float) * (size_t)(lut_len + 1));
     orc_lut_table(Fs, T);
     T[lut_len] = 0.0f;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
     for (long m = 0; m < M; m++) {
         double *h = rir + m * ld;
         for (int t = 0; t < nISM; t++) h[t] = 0.0;
