@@ -50,8 +50,8 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the batched / adjoint / trajectory measurements")
-    p.add_argument("--extras", default="batched,inverse,trajectory",
-                   help="comma list of the extra measurements to run (batched, inverse, trajectory)")
+    p.add_argument("--extras", default="batched,inverse,trajectory,tuning",
+                   help="comma list of the extra measurements to run (batched, inverse, trajectory, tuning)")
     return p.parse_args()
 
 
@@ -231,7 +231,7 @@ def _timed(fn, steps, stream, flush=None):
     return ts[len(ts) // 2]
 
 
-def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory")):
+def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory", "tuning")):
     """The metric's other parts: batched vs plain forward (512 uneven rooms), forward +
     adjoint step vs forward (16 rooms x 32 RIRs), trajectory filtering (400 points)."""
     import torch
@@ -246,7 +246,47 @@ def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory")):
         out.update(_extra_inverse(workloads, sim, flush, stream, fs, dev))
     if "trajectory" in which:
         out.update(_extra_trajectory(workloads, sim, flush, stream, fs, dev))
+    if "tuning" in which:
+        out.update(_extra_tuning(G, B, workloads, flush, stream, fs, dev))
     return out
+
+
+def _extra_tuning(G, B, workloads, flush, stream, fs, dev):
+    """The autotuner on this GPU, then the batched-rooms replay and the fused
+    inverse-problem step with the default and with the tuned launch shapes."""
+    import torch
+    from gpurir_gb300 import tune
+    from gpurir_gb300.autograd import TorchBatch
+    entry = tune.tune(reps=5, warmup=2, write=False)
+    rooms = workloads.batched_rooms()
+    inv = workloads.inverse_problem()
+    t = lambda a, g=False: torch.tensor(a, device=dev, requires_grad=g)
+    beta = t(np.stack([r["beta"] for r in inv]), True)
+    ps = t(np.concatenate([r["pos_src"] for r in inv]))
+    pr = t(np.concatenate([r["pos_rcv"] for r in inv]))
+    orv = t(np.concatenate([r["orV_rcv"] for r in inv]))
+    res = {}
+    for label, knobs in (("default", None), ("tuned", entry["knobs"])):
+        tune.reset()
+        if knobs:
+            tune.set_knobs(knobs)
+        sim = G.Simulator(seed=9)
+        plan = B.BatchPlan(rooms, fs, sim=sim)
+        for _ in range(2):
+            plan.launch(stream.cuda_stream)
+        tb = _timed(lambda: plan.launch(stream.cuda_stream), 10, stream, flush)
+        model = TorchBatch(inv, fs, sim=sim)
+        target = model(beta.detach() * 0.99, ps, pr, None, orv).detach()
+        for _ in range(3):
+            model.l2_step(beta, ps, pr, None, orv, target)
+        ti = _timed(lambda: model.l2_step(beta, ps, pr, None, orv, target), 20, stream, flush)
+        res[label] = {"batched_ms": tb, "inverse_l2_step_ms": ti}
+        del plan, model
+    tune.reset()
+    return {"tuning": {"knobs": entry["knobs"], "candidates_ms": entry["timings_ms"], "tuned_s": entry["tuned_s"],
+                       "default": res["default"], "tuned": res["tuned"],
+                       "note": "launch-shape knobs only (results bitwise equal for every candidate); "
+                               "batched = 512-room graph replay, inverse = fused L2 step"}}
 
 
 def _extra_batched(G, B, workloads, sim, flush, stream, fs, dev):

@@ -109,6 +109,8 @@ class Simulator:
 
     def __init__(self, mixed_precision=False, lut=False, seed=1234, reference_delays=False):
         self._L = _lib.load()
+        from . import tune
+        tune.apply_cached_once()   # launch shapes measured on this GPU, if cached
         h = ctypes.c_void_p()
         _lib.check(self._L.gpurir_create(int(mixed_precision), int(lut), int(seed),
                                          ctypes.byref(h)), "gpurir_create")

@@ -52,6 +52,10 @@ SIGNATURES = {
     "gpurir_host_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
     "gpurir_host_free": (c_int, [c_void_p]),
     "gpurir_probe_peaks": (c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "gpurir_set_tuning": (c_int, [ctypes.c_char_p, c_int]),
+    "gpurir_get_tuning": (c_int, [ctypes.c_char_p, iptr]),
+    "gpurir_reset_tuning": (c_int, []),
+    "gpurir_device_name": (c_int, [ctypes.c_char_p, c_int]),
 }
 
 

@@ -65,6 +65,7 @@ cudaError_t traj_adjoint_launch(const double *g, long n_out, const int *w_ini, c
                                 float *grad_rir, float *grad_sig, float2 *acc, int grid, cudaStream_t st);
 cudaError_t room_beta_launch(RoomDesc *rooms, int n_rooms, const float *beta, cudaStream_t st);
 int l2_grad_blocks(long n);
+int tuning(int knob);
 cudaError_t l2_grad_launch(const float *y, const float *t, long n, float scale, float *g, double *partial,
                            float *loss, cudaStream_t st);
 cudaError_t room_beta_skip_launch(RoomDesc *rooms, int n_rooms, const float *beta, const IsmItem *items,
@@ -555,6 +556,7 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
     size_t smem = ism_forward_smem_bytes(P.tpl, P.em, P.nsub, P.mode, P.tw);
     int bps = ism_forward_blocks_per_sm(P.tpl, smem, P.mode);
     if (bps < 1) return fail(GPURIR_ERR_CUDA, "ISM kernel does not fit on an SM");
+    if (tuning(1) > 0) bps = std::min(bps, tuning(1));   // ism_blocks_per_sm (tuning.cu)
     P.grid = (int)std::min<long>((long)P.items.size(), (long)s->num_sms * bps);
     return GPURIR_OK;
 }
@@ -612,6 +614,7 @@ static std::vector<double> plan_key(const gpurir_sim *s, const std::vector<RoomD
     k.reserve(4 + 16 * R.size());
     k.push_back((double)s->mp);
     k.push_back((double)s->lut);
+    k.push_back((double)tuning(1));   // the launch shape follows ism_blocks_per_sm
     k.push_back(host_io ? 1.0 : 0.0);
     k.push_back((double)out_elems);
     for (const RoomDesc &r : R) {
@@ -1163,6 +1166,7 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
         if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
         bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, smem);
         if (bps < 1) return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
+        if (tuning(2) > 0) bps = std::min(bps, tuning(2));   // adjoint_blocks_per_sm (tuning.cu)
     }
     const std::vector<IsmItem> &bi = P.items;
     const int n_items = (int)bi.size();
@@ -1275,6 +1279,7 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
             delete a;
             return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
         }
+        if (tuning(2) > 0) bps = std::min(bps, tuning(2));   // adjoint_blocks_per_sm (tuning.cu)
     }
     const int n_items = (int)P.items.size();
     a->grid_b = std::min(n_items, s->num_sms * bps);

@@ -631,10 +631,13 @@ __global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / RO
     }
 }
 
-template <int M>
-static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S, const float2 *W,
-                                   const float2 *Sg, float *out, long out_ld, cudaStream_t st) {
-    constexpr int ROWS = kConvRows;
+int tuning(int knob);
+constexpr int kTuneConvRowsKnob = 0;   // TuneKnob::kTuneConvRows (tuning.cu)
+constexpr int kTuneTrajBlocksKnob = 3; // TuneKnob::kTuneTrajBlocksPerSm
+
+template <int M, int ROWS>
+static cudaError_t launch_reg_conv_rows(const float *rir, int P, int R, int L, int S, const float2 *W,
+                                        const float2 *Sg, float *out, long out_ld, cudaStream_t st) {
     const size_t smem = (size_t)ROWS * (M + M / 16) * sizeof(float2);
     static int blocks = -1;
     if (blocks < 0) {
@@ -651,6 +654,16 @@ static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S,
     const int grid = std::min((P * R + ROWS - 1) / ROWS, blocks);
     rir_conv_reg_kernel<M, ROWS><<<grid, M / 16, smem, st>>>(rir, P, R, L, S, W, Sg, out, out_ld);
     return cudaGetLastError();
+}
+
+// Rows per block from the tuning table (1: more blocks per SM; 2: twiddles and
+// barriers shared by a pair of rows).  Each row's arithmetic is the same either way.
+template <int M>
+static cudaError_t launch_reg_conv(const float *rir, int P, int R, int L, int S, const float2 *W,
+                                   const float2 *Sg, float *out, long out_ld, cudaStream_t st) {
+    if (tuning(kTuneConvRowsKnob) == 1)
+        return launch_reg_conv_rows<M, 1>(rir, P, R, L, S, W, Sg, out, out_ld, st);
+    return launch_reg_conv_rows<M, kConvRows>(rir, P, R, L, S, W, Sg, out, out_ld, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -808,8 +821,9 @@ static cudaError_t launch_traj_adjoint(const float *gt, long n_out, const int *w
 // Blocks of the adjoint kernel for FFT half-size M (one per SM at most: the kernel
 // holds two padded rows of shared memory).
 int traj_adjoint_grid(int M, int P, int num_sms) {
-    (void)M;
-    return std::max(1, std::min(P, num_sms * (M <= 4096 ? 2 : 1)));
+    const int t = tuning(kTuneTrajBlocksKnob);
+    const int per_sm = t > 0 ? t : (M <= 4096 ? 2 : 1);
+    return std::max(1, std::min(P, num_sms * per_sm));
 }
 
 cudaError_t traj_adjoint_launch(const double *g, long n_out, const int *w_ini, const int *w_len, const float *rir,

@@ -343,6 +343,23 @@ int gpurir_last_timing(gpurir_sim *sim, float *ism_ms, float *tail_ms);
  * entry the RIRs).  No counterpart in the reference. */
 int gpurir_last_transfer_bytes(gpurir_sim *sim, uint64_t *h2d, uint64_t *d2h);
 
+/* Launch-shape tuning knobs, process-wide: "conv_rows" (1 or 2 RIR rows per
+ * block of the convolution), "ism_blocks_per_sm" (resident blocks of the forward
+ * ISM kernel, 0 = as many as fit), "adjoint_blocks_per_sm" (same for the adjoint
+ * kernel), "traj_adjoint_blocks_per_sm" (trajectory adjoint, 0 = by FFT size).
+ * No knob changes any result bit: they choose how work is laid out on the GPU,
+ * not the arithmetic.  Batches and adjoint handles created before a change keep
+ * their launch shape; simulate calls plan again.  The
+ * autotuner (gpurir_gb300/tune.py) picks them per GPU and caches them on disk.
+ * The reference fixes these choices at compile time (src/gpuRIR_cuda.cu:20-45). */
+int gpurir_set_tuning(const char *knob, int value);
+int gpurir_get_tuning(const char *knob, int *value);
+int gpurir_reset_tuning(void);
+
+/* Name of the current device with its compute capability and SM count (the key
+ * of the autotuner's cache), into name[len]. */
+int gpurir_device_name(char *name, int len);
+
 /* Measured throughput of this device's FP32 FMA pipe (FLOP/s, 2 per FMA) and
  * MUFU pipe (reciprocals/s): the peaks of the sinc-accumulation roofline.
  * No counterpart in the reference (which has no roofline accounting). */
