@@ -149,6 +149,11 @@ class Simulator:
                    "reference_delays")
         return bool(st.value)
 
+    def set_compensation(self, policy):
+        """Compensated accumulation: 0 never, 1 long RIRs in lookup-table mode (default),
+        2 always in mixed-precision and lookup-table modes (gpurir_set_compensation)."""
+        _lib.check(self._L.gpurir_set_compensation(self._h, int(policy)), "set_compensation")
+
     def modes(self):
         mp, lut, rd = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _lib.check(self._L.gpurir_get_modes(self._h, ctypes.byref(mp), ctypes.byref(lut)), "modes")

@@ -31,6 +31,7 @@ SIGNATURES = {
     "gpurir_get_modes": (c_int, [c_void_p, iptr, iptr]),
     "gpurir_set_reference_delays": (c_int, [c_void_p, c_int, iptr]),
     "gpurir_get_reference_delays": (c_int, [c_void_p, iptr]),
+    "gpurir_set_compensation": (c_int, [c_void_p, c_int]),
     "gpurir_set_noise": (c_int, [c_void_p, c_int]),
     "gpurir_set_seed": (c_int, [c_void_p, c_u64, c_u64]),
     "gpurir_get_seed": (c_int, [c_void_p, u64ptr, u64ptr]),

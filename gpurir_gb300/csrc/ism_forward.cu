@@ -82,6 +82,14 @@ struct IsmLaunch {
 //             linear filter of a GB300 texture unit (8-bit weight, rounded half up),
 //             support |x| < floor(Tw/2)
 constexpr int kModeF32 = 0, kModeMP = 1, kModeLUT = 2;
+// Flag added to a mode: compensated accumulation across chunks.  Each chunk's taps
+// still go into the FP32 sub-range buffers (few terms per sample per chunk), and
+// after the chunk every touched word is added into a running (hi, lo) pair by
+// TwoSum (Knuth TAOCP vol. 2, 4.2.2) and cleared, so the error of a late, dense
+// sample stops growing with the number of images that reach it.  Used for the
+// lookup-table mode on long RIRs, and on request in mixed precision (capi.cu
+// gpurir_set_compensation).
+constexpr int kModeComp = 4;
 constexpr int kLutOversamp = 16;
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -175,8 +183,10 @@ __device__ __forceinline__ void scatter_list(float *bs, int origin, const float4
     }
 }
 
-template <int TPL, int MODE>
+template <int TPL, int MODE_ARG>
 __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
+    constexpr int MODE = MODE_ARG & 3;                  // tap evaluation
+    constexpr bool COMP = (MODE_ARG & kModeComp) != 0;  // compensated accumulation across chunks
     constexpr int KS = 32 * TPL;   // taps per image, rounded up to the warp
     constexpr int SUB = KS;        // sub-range length
     constexpr int BUF = SUB + KS;  // words per sub-range buffer
@@ -200,8 +210,12 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     // LUT mode: the table after the largest buffers + pool of this launch, rows of
     // (T[16 col + row], T[16 col + row + 1]) pairs so that lanes read consecutive words.
     const int lut_cols = P.tw + 1;
+    // compensated mode: running sums (hi) and their errors (lo), laid out as buf
+    const int comp_words = COMP ? 2 * P.em + P.max_nsub * BUF : 0;
+    float *hi = buf + 2 * P.em + P.max_nsub * BUF + kPool * (2 * P.em + BUF);
+    float *lo = hi + comp_words;
     float2 *lut = reinterpret_cast<float2 *>(
-        buf + ((2 * P.em + P.max_nsub * BUF + kPool * (2 * P.em + BUF) + 1) & ~1));
+        buf + ((2 * P.em + P.max_nsub * BUF + kPool * (2 * P.em + BUF) + 2 * comp_words + 1) & ~1));
     if (MODE == kModeLUT) {
         // T[j] = Hann x sinc at (j - 8 Tw) / 16, as src/gpuRIR_cuda.cu:578-592 tabulates it
         const int center = 8 * P.tw, lut_len = 16 * P.tw + 1;
@@ -242,6 +256,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         const int slot_words = 2 * P.em + BUF;
         float *pool = buf + buf_words;   // kPool slots of [em | BUF | em]
         for (int i = tid; i < buf_words + kPool * slot_words; i += kThreads) buf[i] = 0.0f;
+        if (COMP)
+            for (int i = tid; i < buf_words; i += kThreads) hi[i] = lo[i] = 0.0f;
 
         // Room and pair constants (uniform across the block).
         const float L0 = R.L[0], L1 = R.L[1], L2 = R.L[2];
@@ -589,6 +605,20 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     }
             }
             __syncthreads();
+            if (COMP) {
+                // this chunk's sums into the running (hi, lo) pairs; only the sub-ranges that
+                // received images (their buffers hold every tap of them) are touched
+                for (int i = tid; i < nsub * BUF; i += kThreads) {
+                    if (sub_cnt[i / BUF] == 0) continue;
+                    const float x = buf[P.em + i];
+                    if (x == 0.0f) continue;
+                    const ff t = ff_two_sum(hi[P.em + i], x);
+                    hi[P.em + i] = t.hi;
+                    lo[P.em + i] += t.lo;
+                    buf[P.em + i] = 0.0f;
+                }
+                __syncthreads();
+            }
         }
         // ---- output: sum of the covering sub-range buffers, ascending s.  An item that
         //      holds a whole early part also predicts the envelope from it and writes the
@@ -617,7 +647,10 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 int num = rel - k_lo - BUF + 1;   // buffer s covers rel in [s*SUB + k_lo, s*SUB + k_lo + BUF)
                 int s_min = num <= 0 ? 0 : (num + SUB - 1) / SUB;
                 float acc = 0.0f;
-                for (int s = s_min; s <= s_max; s++) acc += buf[P.em + s * BUF + rel - s * SUB - k_lo];
+                for (int s = s_min; s <= s_max; s++) {
+                    const int w = P.em + s * BUF + rel - s * SUB - k_lo;
+                    acc += COMP ? hi[w] + lo[w] : buf[w];
+                }
                 v[e] = acc;
             }
             if (vec_out && t0 + 3 < t_hi) {
@@ -663,10 +696,11 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
 // ---------------------------------------------------------------------------
 size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub, int mode, int tw) {
     const int ks = 32 * tpl;
-    size_t words = (size_t)(2 * em + max_nsub * 2 * ks) + (size_t)kPool * (2 * em + 2 * ks);
+    const size_t comp = (mode & kModeComp) ? 2 * (size_t)(2 * em + max_nsub * 2 * ks) : 0;
+    size_t words = (size_t)(2 * em + max_nsub * 2 * ks) + (size_t)kPool * (2 * em + 2 * ks) + comp;
     size_t fixed = kChunk * (sizeof(float4) + sizeof(short) + sizeof(unsigned short) + 1) +
                    (kWarps * kMaxSub + 3 * kMaxSub + kMaxItems + kPool + 8) * sizeof(int);
-    size_t lut = mode == kModeLUT ? (size_t)kLutOversamp * (tw + 1) * sizeof(float2) + sizeof(float) : 0;
+    size_t lut = (mode & 3) == kModeLUT ? (size_t)kLutOversamp * (tw + 1) * sizeof(float2) + sizeof(float) : 0;
     return fixed + words * sizeof(float) + lut;
 }
 
@@ -674,7 +708,8 @@ int ism_forward_max_nsub(int tpl, int em, size_t smem_budget, int mode, int tw) 
     const int ks = 32 * tpl;
     size_t fixed = ism_forward_smem_bytes(tpl, em, 0, mode, tw);
     if (smem_budget <= fixed) return 0;
-    long n = (long)((smem_budget - fixed) / (sizeof(float) * 2 * ks));
+    const size_t per_sub = sizeof(float) * 2 * ks * ((mode & kModeComp) ? 3 : 1);
+    long n = (long)((smem_budget - fixed) / per_sub);
     return (int)(n < kMaxSub ? n : kMaxSub);
 }
 
@@ -734,6 +769,8 @@ int ism_forward_blocks_per_sm(int tpl, size_t smem, int mode) {
     case kModeF32: return occupancy<kModeF32>(tpl, smem);
     case kModeMP: return occupancy<kModeMP>(tpl, smem);
     case kModeLUT: return occupancy<kModeLUT>(tpl, smem);
+    case kModeMP | kModeComp: return occupancy<kModeMP | kModeComp>(tpl, smem);
+    case kModeLUT | kModeComp: return occupancy<kModeLUT | kModeComp>(tpl, smem);
     default: return 0;
     }
 }
@@ -779,6 +816,8 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
     case kModeF32: return launch_mode<kModeF32>(tpl, p, grid, smem, st);
     case kModeMP: return launch_mode<kModeMP>(tpl, p, grid, smem, st);
     case kModeLUT: return launch_mode<kModeLUT>(tpl, p, grid, smem, st);
+    case kModeMP | kModeComp: return launch_mode<kModeMP | kModeComp>(tpl, p, grid, smem, st);
+    case kModeLUT | kModeComp: return launch_mode<kModeLUT | kModeComp>(tpl, p, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -80,6 +80,20 @@ int gpurir_get_modes(gpurir_sim *sim, int *mixed_precision, int *lookup_table);
 int gpurir_set_reference_delays(gpurir_sim *sim, int activate, int *state);
 int gpurir_get_reference_delays(gpurir_sim *sim, int *state);
 
+/* Compensated accumulation of the taps in the mixed-precision and lookup-table
+ * modes: each chunk of images is summed into FP32 buffers as usual, then added
+ * into a running (hi, lo) pair per sample by an error-free two-sum, so the
+ * rounding error of a late, dense sample does not grow with the number of
+ * images reaching it (lookup table at 1 s: 1.9e-7 rel-L2 late in the RIR
+ * instead of 5.8e-7).  policy 0: never; 1 (default): lookup-table mode when an
+ * early part is at least 8000 samples long; 2: always, mixed precision too
+ * (where the half-precision window, 1.3e-4, dominates anyway).  It costs shared
+ * memory (shorter segments: ~1.5x the time on a 1 s RIR), not arithmetic per
+ * tap.  The FP32 mode is not affected.  The
+ * reference accumulates its half2 path in half precision
+ * (src/gpuRIR_cuda.cu:501-506); it has no such switch. */
+int gpurir_set_compensation(gpurir_sim *sim, int policy);
+
 /* Noise transform of the tail (GPURIR_NOISE_*), and the (seed, call counter)
  * pair that keys it.  The counter advances by one per simulate call. */
 int gpurir_set_noise(gpurir_sim *sim, int noise_kind);

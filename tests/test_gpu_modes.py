@@ -73,3 +73,39 @@ def test_mode_flags_exclude_each_other(built):
     assert sim.modes() == dict(mixed_precision=True, lut=False, reference_delays=True)
     sim.activate_reference_delays(False)
     assert sim.modes() == dict(mixed_precision=True, lut=False, reference_delays=False)
+
+
+def _long_room_errors(T, mode, policy):
+    import gpurir_gb300 as G
+    room = [4.0, 3.0, 2.5]
+    ps = np.array([[1.1, 1.3, 1.2]], np.float32)
+    pr = np.array([[2.9, 1.9, 1.4], [3.3, 0.8, 1.9]], np.float32)
+    beta, fs = [0.97] * 6, 16000.0
+    nb = [int(np.ceil(2 * 343 * T / d)) for d in room]
+    amp, tau, _ = oracle.amp_tau(room, beta, ps, pr, nb, fs)
+    n = oracle.n_samples(T, fs)
+    a, t = amp.reshape(2, -1), tau.reshape(2, -1)
+    want = oracle.ism_sum_lut(a, t, n, fs) if mode == "lut" else oracle.ism_sum(a, t, n, fs)
+    sim = G.Simulator(mixed_precision=(mode == "mp"), lut=(mode == "lut"))
+    sim.set_compensation(policy)
+    got = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, T, T, fs).reshape(2, -1)
+    q = 3 * n // 4   # the last quarter: the densest samples
+    return rel_l2(got[:, q:], want[:, q:])
+
+
+def test_compensated_accumulation_on_long_dense_rirs(built):
+    """A small, reverberant room with every image up to T (nb_img = t2n(T)): at
+    0.75 s the lookup-table mode's error late in the RIR, with compensated
+    accumulation (the default for long RIRs), stays where it is at 0.25 s and
+    below the uncompensated error; mixed precision is flat in T (its FP32
+    accumulation never was the bottleneck)."""
+    lut_short = _long_room_errors(0.25, "lut", 1)
+    lut_long = _long_room_errors(0.75, "lut", 1)
+    lut_long_plain = _long_room_errors(0.75, "lut", 0)
+    mp_short = _long_room_errors(0.25, "mp", 1)
+    mp_long = _long_room_errors(0.75, "mp", 2)
+    print("lut %.2e -> %.2e (plain %.2e), mp %.2e -> %.2e" % (lut_short, lut_long, lut_long_plain, mp_short,
+                                                           mp_long))
+    assert lut_long <= 1.3 * lut_short
+    assert lut_long < lut_long_plain
+    assert mp_long <= 1.2 * mp_short
