@@ -481,6 +481,67 @@ __device__ __forceinline__ void reg_fft_rows(float2 (&v)[ROWS][16], float2 *buf,
     __syncthreads();
 }
 
+// For M = 2 * 16^n the last Stockham pass of reg_fft_rows is a radix-2 pass, one more
+// shared-memory round trip and barrier for two additions per element.  The
+// convolution folds it into its spectral step instead (and the inverse's first
+// radix-2 pass likewise): reg_fft_rows_head stops before that pass, leaving the
+// half-size DFTs A = buf[0, M/2) and B = buf[M/2, M) (Z[k] = A[k] + W_M^k B[k],
+// Z[k + M/2] = A[k] - W_M^k B[k]); reg_fft_rows_tail runs the radix-16 passes that
+// follow an external first radix-2 pass (Ns = 2, 32, 512, ...).
+template <bool INV, int M, int ROWS>
+__device__ __forceinline__ void reg_fft_rows_head(float2 (&v)[ROWS][16], float2 *buf, const float2 *__restrict__ W) {
+    constexpr int T = M / 16, BS = M + M / 16;
+    const int j = threadIdx.x;
+    pass16_rows<INV, M, ROWS>(v, buf, j, 1, W);   // v loaded by the caller
+    __syncthreads();
+    int Ns = 16;
+#pragma unroll 1
+    for (; Ns * 16 <= M; Ns *= 16) {
+#pragma unroll
+        for (int q = 0; q < ROWS; q++)
+#pragma unroll
+            for (int r = 0; r < 16; r++) v[q][r] = buf[q * BS + pad16(j + r * T)];
+        __syncthreads();
+        pass16_rows<INV, M, ROWS>(v, buf, j, Ns, W);
+        __syncthreads();
+    }
+}
+
+template <bool INV, int M, int ROWS>
+__device__ __forceinline__ void reg_fft_rows_tail(float2 (&v)[ROWS][16], float2 *buf, const float2 *__restrict__ W) {
+    constexpr int T = M / 16, BS = M + M / 16;
+    const int j = threadIdx.x;
+#pragma unroll 1
+    for (int Ns = 2; Ns * 16 <= M; Ns *= 16) {
+#pragma unroll
+        for (int q = 0; q < ROWS; q++)
+#pragma unroll
+            for (int r = 0; r < 16; r++) v[q][r] = buf[q * BS + pad16(j + r * T)];
+        __syncthreads();
+        pass16_rows<INV, M, ROWS>(v, buf, j, Ns, W);
+        __syncthreads();
+    }
+}
+
+// Spectral step of one bin pair (k, M - k) of the convolution: real-FFT bins from the
+// packed spectrum values zk = Z[k], zm = Z[(M - k) mod M], times the segment spectrum
+// (sk, sm), repacked for the inverse packed FFT: returns Y'[k] and Y'[M - k].
+__device__ __forceinline__ void conv_bin_pair(float2 zk, float2 zm, float2 wk, float2 sk, float2 sm, float2 &ok,
+                                              float2 &om) {
+    const float2 ze = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    const float2 zo = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    const float2 ze2 = make_float2(ze.x, -ze.y), zo2 = make_float2(zo.x, -zo.y);
+    const float2 wm = make_float2(-wk.x, wk.y);
+    const float2 yk = cmul(cadd(ze, cmul(wk, zo)), sk);
+    const float2 ym = cmul(cadd(ze2, cmul(wm, zo2)), sm);
+    const float2 yec = make_float2(0.5f * (yk.x + ym.x), 0.5f * (yk.y - ym.y));
+    const float2 yod = cmul(make_float2(0.5f * (yk.x - ym.x), 0.5f * (yk.y + ym.y)), cconj(wk));
+    ok = make_float2(yec.x - yod.y, yec.y + yod.x);
+    const float2 yec2 = make_float2(0.5f * (ym.x + yk.x), 0.5f * (ym.y - yk.y));
+    const float2 yod2 = cmul(make_float2(0.5f * (ym.x - yk.x), 0.5f * (ym.y + yk.y)), cconj(wm));
+    om = make_float2(yec2.x - yod2.y, yec2.y + yod2.x);
+}
+
 // Pass-1 inputs of thread j straight from global memory: z[n] = x[2n] + i x[2n+1],
 // n = j + r M/16, zero past `len` (8-byte loads when the row allows).
 template <int M>
@@ -534,6 +595,88 @@ __global__ void __launch_bounds__(M / 16, 16384 / M) segment_spectra_reg_kernel(
     }
 }
 
+// Forward FFT of the rows (v loaded), spectral step and inverse FFT for M = 2 * 16^n, with
+// the forward's last radix-2 pass and the inverse's first one folded into the spectral
+// step.  Unit u in [0, M/4] takes the bins k = u, M - k, k' = M/2 - u, M - k': it reads
+// A[k], B[k], A[k'], B[k'], forms Z[k], Z[k + M/2], Z[k'], Z[k' + M/2] exactly as the
+// radix-2 pass would, does the spectral step of the pairs (k, M - k) and (k', M - k'),
+// and writes the inverse's first radix-2 outputs 2k, 2k + 1, 2k', 2k' + 1.  All reads
+// happen before a barrier and all writes after it (the writes land on other units'
+// inputs); the values wait in v, free between the transforms.
+template <int M, int ROWS>
+__device__ __forceinline__ void conv_spectral_fused(float2 (&v)[ROWS][16], float2 *buf, const float2 *__restrict__ W,
+                                                    const float2 *__restrict__ Sg, int pr0, int nq, int R) {
+    constexpr int T = M / 16, BS = M + M / 16, H = M / 2, Q = M / 4;
+    static_assert(Q == 4 * T, "four units per thread");
+    const int j = threadIdx.x;
+    reg_fft_rows_head<false, M, ROWS>(v, buf, W);
+    float2 e[ROWS][2];   // unit M/4 (thread 0 only): Z[M/4], Z[3M/4]
+#pragma unroll
+    for (int q = 0; q < ROWS; q++) {
+        const float2 *bq = buf + q * BS;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int u = j + i * T;
+            if (u == 0) {   // bins 0 and M/2: Z[0] = A[0] + B[0], Z[M/2] = A[0] - B[0]
+                float2 a0 = bq[pad16(0)], a1 = cmul(bq[pad16(H)], __ldg(&W[0]));
+                v[q][4 * i] = cadd(a0, a1);
+                v[q][4 * i + 1] = csub(a0, a1);
+            } else {
+                const int k = u, kp = H - u;
+                const float2 ak = bq[pad16(k)], bk = cmul(bq[pad16(k + H)], __ldg(&W[2 * k]));
+                const float2 ap = bq[pad16(kp)], bp = cmul(bq[pad16(kp + H)], __ldg(&W[2 * kp]));
+                v[q][4 * i] = cadd(ak, bk);        // Z[k]
+                v[q][4 * i + 1] = csub(ak, bk);    // Z[k + M/2] = Z[M - k']
+                v[q][4 * i + 2] = cadd(ap, bp);    // Z[k']
+                v[q][4 * i + 3] = csub(ap, bp);    // Z[k' + M/2] = Z[M - k]
+            }
+        }
+        if (j == 0) {
+            const float2 a = bq[pad16(Q)], b = cmul(bq[pad16(Q + H)], __ldg(&W[2 * Q]));
+            e[q][0] = cadd(a, b);
+            e[q][1] = csub(a, b);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < ROWS; q++) {
+        if (q >= nq) break;
+        float2 *bq = buf + q * BS;
+        const float2 *sp = Sg + (size_t)((pr0 + q) / R) * (M + 1);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int u = j + i * T;
+            if (u == 0) {
+                float2 y0, yM, yh, yh2;
+                conv_bin_pair(v[q][0], v[q][0], __ldg(&W[0]), __ldg(&sp[0]), __ldg(&sp[M]), y0, yM);
+                conv_bin_pair(v[q][1], v[q][1], __ldg(&W[H]), __ldg(&sp[H]), __ldg(&sp[H]), yh, yh2);
+                bq[pad16(0)] = cadd(y0, yh);
+                bq[pad16(1)] = csub(y0, yh);
+            } else {
+                const int k = u, kp = H - u;
+                float2 yk, ymk, ykp, ymkp;
+                // pair (k, M - k): Z[k], Z[M - k] = Z[k' + M/2]; pair (k', M - k'): Z[k'], Z[k + M/2]
+                conv_bin_pair(v[q][4 * i], v[q][4 * i + 3], __ldg(&W[k]), __ldg(&sp[k]), __ldg(&sp[M - k]), yk, ymk);
+                conv_bin_pair(v[q][4 * i + 2], v[q][4 * i + 1], __ldg(&W[kp]), __ldg(&sp[kp]), __ldg(&sp[M - kp]),
+                              ykp, ymkp);
+                // the inverse's first radix-2 pass: out[2j] = Y'[j] + Y'[j + M/2], out[2j + 1] = difference
+                bq[pad16(2 * k)] = cadd(yk, ymkp);        // Y'[k + M/2] = Y'[M - k']
+                bq[pad16(2 * k + 1)] = csub(yk, ymkp);
+                bq[pad16(2 * kp)] = cadd(ykp, ymk);       // Y'[k' + M/2] = Y'[M - k]
+                bq[pad16(2 * kp + 1)] = csub(ykp, ymk);
+            }
+        }
+        if (j == 0) {
+            float2 yq, y3q;
+            conv_bin_pair(e[q][0], e[q][1], __ldg(&W[Q]), __ldg(&sp[Q]), __ldg(&sp[M - Q]), yq, y3q);
+            bq[pad16(2 * Q)] = cadd(yq, y3q);
+            bq[pad16(2 * Q + 1)] = csub(yq, y3q);
+        }
+    }
+    __syncthreads();
+    reg_fft_rows_tail<true, M, ROWS>(v, buf, W);
+}
+
 template <int M, int ROWS>
 __global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / ROWS : 1)) rir_conv_reg_kernel(
         const float *__restrict__ rir, int P, int R, int L, int S, const float2 *__restrict__ W,
@@ -567,6 +710,9 @@ __global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / RO
                 for (int r = 0; r < 16; r++) v[q][r] = make_float2(0.0f, 0.0f);
             }
         }
+        if constexpr (M == 8192) {
+            conv_spectral_fused<M, ROWS>(v, buf, W, Sg, pr0, nq, R);
+        } else {
         reg_fft_rows<false, M, true, ROWS>(v, buf, W);
         // spectrum of the RIR at k and M - k, times the segment's spectrum, repacked
         // for the inverse real FFT (same algebra as rir_conv_kernel).  The thread's k are
@@ -612,6 +758,7 @@ __global__ void __launch_bounds__(M / 16, (16384 / M / ROWS > 0 ? 16384 / M / RO
         }
         __syncthreads();
         reg_fft_rows<true, M, false, ROWS>(v, buf, W);
+        }
         for (int q = 0; q < nq; q++) {
             const float2 *bq = buf + q * BS;
             float *o = out + (size_t)(pr0 + q) * out_ld;
