@@ -73,6 +73,21 @@ __device__ __forceinline__ void tail_fill(float *trow, int n_diff, int s_begin, 
     const bool vec4 = ((reinterpret_cast<uintptr_t>(trow) & 15) == 0);
     const float step = __expf(ea);   // envelope ratio between consecutive samples
     const int end = min(s_end, n_diff);
+    if (eb == -INFINITY) {
+        // silent envelope (A = 0: no image energy in the envelope window): every sample is
+        // 0 * finite noise, so the noise is not drawn
+#pragma unroll 1
+        for (int s = s_begin + 4 * tid; s < end; s += 4 * nthreads) {
+            if (vec4 && s + 3 < end) {
+                *reinterpret_cast<float4 *>(trow + s) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (s + e < end) trow[s + e] = 0.0f;
+            }
+        }
+        return;
+    }
 #pragma unroll 1
     for (int s = s_begin + 4 * tid; s < end; s += 4 * nthreads) {
         const uint4 w = philox4x32_10(make_uint4((uint32_t)(s >> 2), rir, off_lo, off_hi), key);
