@@ -338,3 +338,38 @@ def test_live_reference_kernels_random_scenes(built):
         _, rm = _engine(sc, "mp", reference_delays=True)
         assert rel_l2(rm[..., :n], mp["early"]) < 2e-3
     rk.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not ref_kernels.available(), reason="reference kernels not built (oracle/_ref)")
+def test_tail_energy_decay_matches_reference_kernels(built):
+    """The engine's diffuse tail (Philox, logistic transform) against the reference's
+    own tail: its envPred_kernel and diffRev_kernel run live (src/gpuRIR_cuda.cu:
+    415-461) on uniforms standing in for its cuRAND stream (a closed library).  The
+    noise differs, the statistics must not: the energy-decay curve (Schroeder
+    integral) averaged over the 16 RIRs agrees within 0.5 dB down to -60 dB, up to
+    2 / |alpha| samples before the end (where a few samples decide the integral)."""
+    import torch
+    import gpurir_gb300 as G
+    rng = np.random.default_rng(5)
+    room = [6.0, 5.0, 3.0]
+    beta = G.beta_SabineEstimation(room, 1.0)
+    ps = (0.5 + rng.random((4, 3)) * (np.array(room) - 1)).astype(np.float32)
+    pr = (0.5 + rng.random((4, 3)) * (np.array(room) - 1)).astype(np.float32)
+    nb, fs, Tdiff, Tmax = G.t2n(0.1, room), 16000.0, 0.1, 1.0
+    rk = ref_kernels.RefKernels()
+    n_ism, n = oracle.n_samples(Tdiff, fs), oracle.n_samples(Tmax, fs)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    u = torch.rand((16 * (n - n_ism),), device="cuda", generator=g).clamp_(1e-7, 1 - 1e-7)
+    ref = rk.simulate(room, beta, ps, pr, nb, Tmax, fs, Tdiff=Tdiff, mode="fp32", uniforms=u)
+    rk.close()
+    ref_rir = np.concatenate([ref["early"], ref["diffuse"]], axis=-1).reshape(16, n).astype(np.float64)
+    sim = G.Simulator(seed=8, reference_delays=True)
+    got = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, Tdiff, Tmax, fs).reshape(16, n)
+    edc = lambda x: np.mean([np.cumsum((r.astype(np.float64) ** 2)[::-1])[::-1] for r in x], axis=0)
+    ea, eb = edc(got), edc(ref_rir)
+    alpha = abs(float(ref["alpha"].ravel()[0]))
+    keep = (eb > eb[0] * 1e-6) & (np.arange(n) < n - int(2 / alpha))
+    d = 10 * np.log10(ea[keep] / eb[keep])
+    print("EDC max difference %.3f dB over %d samples" % (np.abs(d).max(), keep.sum()))
+    assert np.abs(d).max() < 0.5
