@@ -112,7 +112,27 @@ __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], c
                                              const float (&sk)[TPL], float al, float4 r, float H,
                                              const float2 *lut, int lut_cols) {
     const float f = r.y;
-    if (MODE == kModeF32) {
+    if (MODE == kModeF32 && (TPL % 2) == 0 && TPL <= 12) {   // (more taps per lane: register spills)
+        // taps i and i + 1 of the lane in packed FP32 (Blackwell's two-wide FADD/FFMA,
+        // each half rounded as the scalar instruction): the image's values are
+        // duplicated once, the lane constants pair up as they lie in registers
+        const float2 f2 = make_float2(-f, -f), ac2 = make_float2(r.z, r.z), as2 = make_float2(r.w, r.w);
+        const float2 al2 = make_float2(al, al);
+#pragma unroll
+        for (int i = 0; i < TPL; i += 2) {
+            const float2 x = __fadd2_rn(make_float2(kf[i], kf[i + 1]), f2);
+            float2 u = __ffma2_rn(make_float2(ck[i], ck[i + 1]), ac2,
+                                  __ffma2_rn(make_float2(sk[i], sk[i + 1]), as2, al2));
+            if (CLAMP) {
+                u.x = fabsf(x.x) < H ? u.x : 0.0f;
+                u.y = fabsf(x.y) < H ? u.y : 0.0f;
+            }
+            const float2 acc = __ffma2_rn(u, make_float2(rcp_approx(x.x), rcp_approx(x.y)),
+                                          make_float2(p[32 * i], p[32 * (i + 1)]));
+            p[32 * i] = acc.x;
+            p[32 * (i + 1)] = acc.y;
+        }
+    } else if (MODE == kModeF32) {
         const float ac = r.z, as = r.w;   // a cos phi, a sin phi
 #pragma unroll
         for (int i = 0; i < TPL; i++) {
