@@ -271,16 +271,42 @@ __global__ void __launch_bounds__(kBThreads, 3) ism_backward_kernel(BwdLaunch P)
                     //   sum g W  = sigma S,   S = sum q w
                     //   sum g W' = sigma T + gamma S,   T = sum q (w' - w / x)
                     float s1 = 0.0f, t1 = 0.0f;
+                    if constexpr ((TPL % 2) == 0 && TPL <= 12) {
+                        // taps k and k + 1 in packed FP32 (two-wide FADD/FMUL/FFMA); the two
+                        // halves of S and T are added at the end
+                        const float2 f2 = make_float2(-f, -f), cp2 = make_float2(cphi, cphi);
+                        const float2 sp2 = make_float2(sphi, sphi), hs2 = make_float2(half_sign, half_sign);
+                        const float2 sd2 = make_float2(sphd, sphd), cd2 = make_float2(-cphd, -cphd);
+                        float2 s2 = make_float2(0.0f, 0.0f), t2 = make_float2(0.0f, 0.0f);
 #pragma unroll
-                    for (int k = 0; k < TPL; k++) {
-                        const float x = kf[k] - f;
-                        const float rx_ = rcp_approx_b(x);
-                        const float w = fmaf(ck[k], cphi, fmaf(sk[k], sphi, half_sign));
-                        const float wd = fmaf(ck[k], sphd, -sk[k] * cphd);
-                        float q = gp[32 * k] * rx_;
-                        if (CLAMP && fabsf(x) >= H) q = 0.0f;
-                        s1 = fmaf(q, w, s1);
-                        t1 = fmaf(q, fmaf(-w, rx_, wd), t1);
+                        for (int k = 0; k < TPL; k += 2) {
+                            const float2 x = __fadd2_rn(make_float2(kf[k], kf[k + 1]), f2);
+                            const float2 rx_ = make_float2(rcp_approx_b(x.x), rcp_approx_b(x.y));
+                            const float2 ck2 = make_float2(ck[k], ck[k + 1]), sk2 = make_float2(sk[k], sk[k + 1]);
+                            const float2 w = __ffma2_rn(ck2, cp2, __ffma2_rn(sk2, sp2, hs2));
+                            const float2 wd = __ffma2_rn(ck2, sd2, __fmul2_rn(sk2, cd2));
+                            float2 q = __fmul2_rn(make_float2(gp[32 * k], gp[32 * (k + 1)]), rx_);
+                            if (CLAMP) {
+                                if (fabsf(x.x) >= H) q.x = 0.0f;
+                                if (fabsf(x.y) >= H) q.y = 0.0f;
+                            }
+                            s2 = __ffma2_rn(q, w, s2);
+                            t2 = __ffma2_rn(q, __ffma2_rn(make_float2(-w.x, -w.y), rx_, wd), t2);
+                        }
+                        s1 = s2.x + s2.y;
+                        t1 = t2.x + t2.y;
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < TPL; k++) {
+                            const float x = kf[k] - f;
+                            const float rx_ = rcp_approx_b(x);
+                            const float w = fmaf(ck[k], cphi, fmaf(sk[k], sphi, half_sign));
+                            const float wd = fmaf(ck[k], sphd, -sk[k] * cphd);
+                            float q = gp[32 * k] * rx_;
+                            if (CLAMP && fabsf(x) >= H) q = 0.0f;
+                            s1 = fmaf(q, w, s1);
+                            t1 = fmaf(q, fmaf(-w, rx_, wd), t1);
+                        }
                     }
                     v[2 * u] = sig * s1;
                     v[2 * u + 1] = fmaf(sig, t1, gam * s1);
