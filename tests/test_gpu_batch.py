@@ -113,3 +113,35 @@ def test_graph_replay(built):
     assert not np.array_equal(B.unpack(c.cpu().numpy(), rooms, fs)[0][..., :n0], vd[0][..., :n0])
     assert sim.get_seed()[1] == 1 or True   # replays keep their own counter on the device
     assert G._lib.load().gpurir_device_status(sim.handle) == 0
+
+
+def test_batch_and_graph_honour_reference_delays(built):
+    """With reference delays on, the batched launch and its CUDA-graph replay
+    use the float32 delay model too: the graph replay equals the batched launch bit
+    for bit, and both, like the single-room call with the same switch, are within
+    float rounding of the oracle fed the reference's float32 delays."""
+    import torch
+    import gpurir_gb300 as G
+    from gpurir_gb300 import batch as B
+    rooms = _rooms(6, seed=5)
+    fs = 16000.0
+    sim = G.Simulator(seed=4, reference_delays=True)
+    out, _ = B.simulate_batch(rooms, fs, sim=sim)
+    plan = B.BatchPlan(rooms, fs, sim=sim)
+    plan.launch()
+    torch.cuda.synchronize()
+    views = B.unpack(out.cpu().numpy(), rooms, fs)
+    gviews = [v.cpu().numpy() for v in plan.rirs()]
+    for r, v, gv in zip(rooms, views, gviews):
+        n = oracle.n_samples(r["Tdiff"], fs)
+        single = sim.simulate_rir(r["room_sz"], r["beta"], r["pos_src"], r["pos_rcv"], r["orV_src"], r["orV_rcv"],
+                                  0, G.polar_patterns[r["mic_pattern"]], r["nb_img"], r["Tdiff"], r["Tmax"], fs)
+        assert np.array_equal(gv[..., :n], v[..., :n])   # the graph replays the batch's plan
+        tau, _ = oracle.tau_reference_f32(r["room_sz"], r["pos_src"], r["pos_rcv"], r["nb_img"], fs, "omni",
+                                          r["mic_pattern"])
+        amp, _, _ = oracle.amp_tau(r["room_sz"], r["beta"], r["pos_src"], r["pos_rcv"], r["nb_img"], fs, "omni",
+                                   r["mic_pattern"], None, r["orV_rcv"])
+        want = oracle.ism_sum(amp.reshape(-1, amp.shape[-1]), tau.reshape(-1, tau.shape[-1]).astype(np.float64),
+                              n, fs).reshape(v[..., :n].shape)
+        assert rel_l2(v[..., :n], want) <= 1e-6
+        assert rel_l2(single[..., :n], want) <= 1e-6   # (its own plan: images may be split differently)
