@@ -340,6 +340,42 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         }
         const float keep_lo = (float)t_lo - H, keep_hi = (float)t_hi + H;
 
+        // a partial item writes its segment at part_off (sample t_lo first)
+        float *orow = it.part_off >= 0 ? P.partial + it.part_off - t_lo : P.out + it.out_row;
+        const bool fuse = P.fuse_tail && it.part_off < 0 && t_lo == 0 && t_hi == R.n_ism &&
+                          R.n_total > R.n_ism;
+        float tau_dp = 0.0f;
+        int w_start = t_hi;
+        if (fuse) {
+            tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
+            w_start = envelope_start(R, tau_dp);
+        }
+        // When no image of the pair can reach the envelope window [w_start, nISM), the
+        // window's samples are exact zeros, the envelope is A = 0 and the tail is silent
+        // whatever the rest of the early part holds.  An item of the first wave (the
+        // first gridDim.x handed out) writes such a tail now, the same values as after
+        // the early part: while the first items compute nothing else is being stored,
+        // so these stores (over the host link when the caller's buffer is in host
+        // memory) overlap the tap work.  Later items keep the tail for the end, where
+        // earlier items' stores already keep the link busy (mic_array into host memory:
+        // 0.79 ms instead of 0.83 ms; no change into HBM).
+        bool tail_written = false;
+        if (fuse && item_id < (int)gridDim.x) {
+            const float s3[3] = {sx, sy, sz}, r3[3] = {rx, ry, rz};
+            if (images_miss_segment(R.L, R.nb, s3, r3, R.kh, H, w_start, R.n_ism)) {
+                const TailEnv e = tail_envelope(R, 0.0f, w_start, tau_dp);
+                if (tid == 0 && P.env_out) {
+                    P.env_out[3 * it.rir] = e.A;
+                    P.env_out[3 * it.rir + 1] = e.alpha;
+                    P.env_out[3 * it.rir + 2] = tau_dp;
+                }
+                const uint64_t offset = P.offset_ptr ? *P.offset_ptr : P.offset;
+                tail_fill(orow + R.n_ism, R.n_total - R.n_ism, 0, R.n_total - R.n_ism, tid, kThreads, e.ea,
+                          e.eb, P.seed, offset, (uint32_t)it.rir, P.noise_kind);
+                tail_written = true;
+            }
+        }
+
         // Per-lane tap constants: k = k_lo + lane + 32 i, sign (-1)^k.
         float kf[TPL], ck[TPL], sk[TPL];
 #pragma unroll
@@ -642,17 +678,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         }
         // ---- output: sum of the covering sub-range buffers, ascending s.  An item that
         //      holds a whole early part also predicts the envelope from it and writes the
-        //      diffuse tail, so those stores overlap other blocks' tap work.
-        // a partial item writes its segment at part_off (sample t_lo first)
-        float *orow = it.part_off >= 0 ? P.partial + it.part_off - t_lo : P.out + it.out_row;
-        const bool fuse = P.fuse_tail && it.part_off < 0 && t_lo == 0 && t_hi == R.n_ism &&
-                          R.n_total > R.n_ism;
-        float tau_dp = 0.0f;
-        int w_start = t_hi;
-        if (fuse) {
-            tau_dp = direct_tau(R, P.pos_src + 3 * it.src, P.pos_rcv + 3 * it.rcv);
-            w_start = envelope_start(R, tau_dp);
-        }
+        //      diffuse tail (unless written above), so those stores overlap other blocks'
+        //      tap work.
         // four consecutive samples per thread (t_lo is a multiple of 4): 16-byte stores
         // where the row allows, which also suits stores into host memory
         float pw = 0.0f;
@@ -684,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
             for (int e = 0; e < 4; e++)
                 if (t0 + e >= w_start && t0 + e < t_hi) pw = fmaf(v[e], v[e], pw);
         }
-        if (fuse) {
+        if (fuse && !tail_written) {
             float *red = reinterpret_cast<float *>(hist);   // free until the next item
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) pw += __shfl_xor_sync(0xffffffffu, pw, o);
