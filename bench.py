@@ -396,13 +396,30 @@ def _extra_inverse(workloads, sim, flush, stream, fs, dev):
     for _ in range(3):
         fused_step()
     t_fused = _timed(fused_step, 20, stream, flush)
+
+    # what one backward() call costs PyTorch itself on this host, whatever the graph:
+    # a trivial loss of a leaf tensor of the same size (host-bound, no kernel of ours)
+    leaf = torch.zeros(model.total, device=dev, requires_grad=True)
+
+    def trivial_bwd():
+        (leaf * 2.0).sum().backward()
+
+    for _ in range(3):
+        trivial_bwd()
+    t_triv = _timed(trivial_bwd, 20, stream, flush)
     out["inverse_problem"] = {"rirs": 16 * 32, "forward_ms": t_f, "forward_adjoint_ms": t_fb,
                               "adjoint_over_forward": t_fb / t_f,
                               "graph_forward_ms": t_gf, "graph_forward_adjoint_ms": t_gfb,
                               "graph_adjoint_over_forward": t_gfb / t_gf,
                               "fused_l2_step_ms": t_fused, "fused_l2_step_over_forward": t_fused / t_f,
+                              "torch_trivial_backward_ms": t_triv,
                               "note": "grads of an L2 loss w.r.t. beta[16,6], pos_src[64,3], "
-                                      "pos_rcv[128,3]; beta stays on the device (TorchBatch)"}
+                                      "pos_rcv[128,3]; beta stays on the device (TorchBatch). "
+                                      "forward_adjoint_ms is the eager autograd step (model, "
+                                      "mse_loss, backward()): host-bound, and "
+                                      "torch_trivial_backward_ms, one backward() of (x * 2).sum() "
+                                      "on a leaf, is what PyTorch alone spends per backward() "
+                                      "call on this host"}
     return out
 
 
