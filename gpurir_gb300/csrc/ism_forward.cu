@@ -182,23 +182,21 @@ __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], c
 
 template <int TPL, bool CLAMP, int MODE>
 __device__ __forceinline__ void scatter_list(float *bs, int origin, const float4 *rec, const short *rec_n0,
-                                             const unsigned short *perm, int j0, int j1,
+                                             int j0, int j1,
                                              const float (&kf)[TPL], const float (&ck)[TPL],
                                              const float (&sk)[TPL], float lane_sign, float H,
                                              const float2 *lut, int lut_cols) {
     int j = j0;
 #pragma unroll 1
     for (; j + 1 < j1; j += 2) {   // two images per trip: half the loop bookkeeping
-        const int ia = perm[j], ib = perm[j + 1];
-        const float4 a = rec[ia], b = rec[ib];
-        const int na = rec_n0[ia], nb = rec_n0[ib];
+        const float4 a = rec[j], b = rec[j + 1];
+        const int na = rec_n0[j], nb = rec_n0[j + 1];
         scatter_taps<TPL, CLAMP, MODE>(bs + (na - origin), kf, ck, sk, a.x * lane_sign, a, H, lut, lut_cols);
         scatter_taps<TPL, CLAMP, MODE>(bs + (nb - origin), kf, ck, sk, b.x * lane_sign, b, H, lut, lut_cols);
     }
     if (j < j1) {
-        const int ia = perm[j];
-        const float4 a = rec[ia];
-        scatter_taps<TPL, CLAMP, MODE>(bs + (rec_n0[ia] - origin), kf, ck, sk, a.x * lane_sign, a, H, lut,
+        const float4 a = rec[j];
+        scatter_taps<TPL, CLAMP, MODE>(bs + (rec_n0[j] - origin), kf, ck, sk, a.x * lane_sign, a, H, lut,
                                        lut_cols);
     }
 }
@@ -214,9 +212,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4 *rec = reinterpret_cast<float4 *>(smem_raw);            // [kChunk] a, f, cos phi, sin phi
     short *rec_n0 = reinterpret_cast<short *>(rec + kChunk);        // [kChunk] floor(tau) - t_lo
-    unsigned short *perm = reinterpret_cast<unsigned short *>(rec_n0 + kChunk);  // [kChunk]
     // [kChunk] rank of the image among its warp's images of the same sub-range (< kPerWarp)
-    unsigned char *rec_rank = reinterpret_cast<unsigned char *>(perm + kChunk);
+    unsigned char *rec_rank = reinterpret_cast<unsigned char *>(rec_n0 + kChunk);
     int *hist = reinterpret_cast<int *>(rec_rank + kChunk);         // [kWarps][kMaxSub]
     int *sub_start = hist + kWarps * kMaxSub;
     int *sub_cnt = sub_start + kMaxSub;
@@ -599,15 +596,32 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                 }
             }
             __syncthreads();
-            // ---- pass 2: stable permutation into sub-range order
-#pragma unroll 1
-            for (int r = 0; r < kRounds; r++) {
-                const int local = warp * kPerWarp + r * 32 + lane;
-                const int rel = rec_n0[local];
-                if (rel != kNoImage) {   // the sub-range as pass 1 derived it from rel
-                    const int sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
-                    perm[my_hist[sub] + rec_rank[local]] = (unsigned short)local;
+            // ---- pass 2: stable permutation into sub-range order, in place: each thread
+            //      holds its images' records in registers across a barrier, then stores
+            //      them at their sorted positions (pass 3 reads them in order)
+            {
+                float4 rv[kRounds];
+                short nv[kRounds];
+                int dst[kRounds];
+#pragma unroll
+                for (int r = 0; r < kRounds; r++) {
+                    const int local = warp * kPerWarp + r * 32 + lane;
+                    const int rel = rec_n0[local];
+                    rv[r] = rec[local];
+                    nv[r] = (short)rel;
+                    dst[r] = -1;
+                    if (rel != kNoImage) {   // the sub-range as pass 1 derived it from rel
+                        const int sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
+                        dst[r] = my_hist[sub] + rec_rank[local];
+                    }
                 }
+                __syncthreads();
+#pragma unroll
+                for (int r = 0; r < kRounds; r++)
+                    if (dst[r] >= 0) {
+                        rec[dst[r]] = rv[r];
+                        rec_n0[dst[r]] = nv[r];
+                    }
             }
             __syncthreads();
             // ---- pass 3: warps pull slices, scatter taps into private buffers
@@ -626,13 +640,13 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                                 P.em + lane;
                     const int origin = s * SUB;   // record n0 is relative to t_lo
                     if (MODE == kModeLUT)   // table values carry their sign: no lane sign
-                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk, 1.0f,
+                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk, 1.0f,
                                                       h_lut, lut, lut_cols);
                     else if (P.clamp)
-                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk,
+                        scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk,
                                                       lane_sign, H, lut, lut_cols);
                     else
-                        scatter_list<TPL, false, MODE>(bs, origin, rec, rec_n0, perm, j0, j1, kf, ck, sk,
+                        scatter_list<TPL, false, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk,
                                                        lane_sign, H, lut, lut_cols);
                 }
             }
@@ -745,7 +759,7 @@ size_t ism_forward_smem_bytes(int tpl, int em, int max_nsub, int mode, int tw) {
     const int ks = 32 * tpl;
     const size_t comp = (mode & kModeComp) ? 2 * (size_t)(2 * em + max_nsub * 2 * ks) : 0;
     size_t words = (size_t)(2 * em + max_nsub * 2 * ks) + (size_t)kPool * (2 * em + 2 * ks) + comp;
-    size_t fixed = kChunk * (sizeof(float4) + sizeof(short) + sizeof(unsigned short) + 1) +
+    size_t fixed = kChunk * (sizeof(float4) + sizeof(short) + 1) +
                    (kWarps * kMaxSub + 3 * kMaxSub + kMaxItems + kPool + 8) * sizeof(int);
     size_t lut = (mode & 3) == kModeLUT ? (size_t)kLutOversamp * (tw + 1) * sizeof(float2) + sizeof(float) : 0;
     return fixed + words * sizeof(float) + lut;
