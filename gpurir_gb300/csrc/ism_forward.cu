@@ -161,6 +161,9 @@ __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], c
         // x = k - f rounds as the reference's t - tau does; texel position
         // __fmaf_rz(x, 16, 8 Tw + 0.5) - 0.5; the upper texel's weight on 8 fractional
         // bits rounded half up, as GB300 texture units filter; border texels are 0.
+        // Without CLAMP every tap has -H < x <= H = Tw/2 (window of exactly 32 TPL taps),
+        // so the texel index lies in [0, 16 Tw] and its clamp changes nothing; the support
+        // test stays (x = H when tau is an integer).
         const float lut_c = (float)(kLutOversamp / 2 * (lut_cols - 1)) + 0.5f;
         const int j_max = kLutOversamp * (lut_cols - 1);
 #pragma unroll
@@ -169,9 +172,11 @@ __device__ __forceinline__ void scatter_taps(float *p, const float (&kf)[TPL], c
             const float xb = __fmaf_rz(x, (float)kLutOversamp, lut_c) - 0.5f;
             const float jf = floorf(xb);
             const float y = (xb - jf) * 256.0f;   // exact
-            const float q = floorf(y);
-            const float w = (q + (y - q >= 0.5f ? 1.0f : 0.0f)) * (1.0f / 256.0f);
-            const int j = min(max((int)jf, 0), j_max);
+            // round half up to 8 bits: floor(y + 1/2), the sum rounded down so that an
+            // inexact y + 1/2 never reaches the next integer
+            const float w = floorf(__fadd_rd(y, 0.5f)) * (1.0f / 256.0f);
+            int j = (int)jf;
+            if (CLAMP) j = min(max(j, 0), j_max);
             const float2 t = lut[(j & (kLutOversamp - 1)) * lut_cols + (j >> 4)];
             float v = fmaf(w, t.y - t.x, t.x);
             v = fabsf(x) < H ? v : 0.0f;
@@ -639,9 +644,12 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     float *bs = (k == 0 ? buf + s * BUF : pool + (pool_base[s] + k - 1) * slot_words) +
                                 P.em + lane;
                     const int origin = s * SUB;   // record n0 is relative to t_lo
-                    if (MODE == kModeLUT)   // table values carry their sign: no lane sign
+                    if (MODE == kModeLUT && P.clamp)   // table values carry their sign: no lane sign
                         scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk, 1.0f,
                                                       h_lut, lut, lut_cols);
+                    else if (MODE == kModeLUT)
+                        scatter_list<TPL, false, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk, 1.0f,
+                                                       h_lut, lut, lut_cols);
                     else if (P.clamp)
                         scatter_list<TPL, true, MODE>(bs, origin, rec, rec_n0, j0, j1, kf, ck, sk,
                                                       lane_sign, H, lut, lut_cols);

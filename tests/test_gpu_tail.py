@@ -94,3 +94,33 @@ def test_empty_envelope_window_gives_silent_tail(built):
     out = sim.simulate_rir(room, [0.9] * 6, ps, pr, None, None, 0, 0, [3, 3, 3], 0.001, 0.1, 16000.0)
     assert np.all(np.isfinite(out))
     assert np.all(out[..., 16:] == 0)
+
+
+def test_silent_tails_of_every_wave_match_the_oracle(built):
+    """More RIRs than the persistent grid holds, every tail silent by geometry (no image
+    reaches the envelope window): the first wave of items writes its tails before the
+    taps, later items after them; both give the oracle's envelope (A = 0) and zeros, and
+    repeated calls are bitwise equal."""
+    import gpurir_gb300 as G
+    rng = np.random.default_rng(13)
+    room = [6.0, 5.0, 3.0]
+    beta = G.beta_SabineEstimation(room, 1.0)
+    ps = _rand_inside(rng, 32, room, 0.5)   # 640 RIRs: one item each, about two waves
+    pr = _rand_inside(rng, 20, room, 0.5)
+    nb, tdiff, tmax, fs = [12, 14, 24], 0.3, 0.6, 16000.0
+    sim = G.Simulator(seed=21)
+    sim.set_noise("gaussian")
+    a = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, tdiff, tmax, fs).copy()
+    assert sim.last_launch_count() == 1   # tails written by the ISM kernel itself
+    env = sim.last_envelope(ps.shape[0] * pr.shape[0])
+    b = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, tdiff, tmax, fs)
+    assert np.array_equal(a, b)
+    ref, p = oracle.simulate_rir(room, beta, ps, pr, nb, tmax, fs, Tdiff=tdiff, seed=21, offset=0,
+                                 noise="gaussian", return_parts=True)
+    n_ism = p["n_ism"]
+    assert np.all(p["A"] == 0)
+    assert np.all(env[:, 0] == 0)
+    assert np.allclose(env[:, 1], p["alpha"].ravel(), rtol=1e-6)
+    assert np.allclose(env[:, 2], p["tau_dp"].ravel(), rtol=1e-6)
+    assert np.all(a[..., n_ism:] == 0)
+    assert rel_l2(a[..., :n_ism], ref[..., :n_ism]) < 1e-6
