@@ -611,7 +611,9 @@ def run_gpu(a):
             "e2e": {"value": e2e_value, "unit": "RIRs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / a.steps * 1e3,
                     "kernel_ms": e2e_kernel_ms / a.steps,
-                    "d2h": "kernel stores into the pinned host buffer over the host link" if direct
+                    "d2h": ("the kernel stores the RIRs into the pinned host buffer over the host "
+                            "link; tails silent by geometry are streamed there meanwhile by a copy "
+                            "engine from a device zero buffer (kernel_ms: the kernel alone)") if direct
                            else "cudaMemcpyAsync after the kernels"},
             "roofline": roofline, "clocks": clk, "gpu_launches": launches, "accuracy": accuracy}
     if world == 1 and not a.no_extras:

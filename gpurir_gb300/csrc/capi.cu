@@ -148,6 +148,11 @@ struct gpurir_sim {
     size_t d_conv_bytes = 0;
     cudaEvent_t conv_busy = nullptr;
     bool conv_recorded = false;
+    // silent tails of host-output calls, streamed by a copy engine from a zero buffer
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_done = nullptr;
+    char *d_zero = nullptr;
+    size_t zero_bytes = 0;
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -194,7 +199,11 @@ extern "C" int gpurir_create(int mixed_precision, int lookup_table, uint64_t see
 extern "C" int gpurir_destroy(gpurir_sim *s) {
     if (!s) return GPURIR_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->side) cudaStreamSynchronize(s->side);
     if (s->d_ws) cudaFree(s->d_ws);
+    if (s->d_zero) cudaFree(s->d_zero);
+    if (s->side_done) cudaEventDestroy(s->side_done);
+    if (s->side) cudaStreamDestroy(s->side);
     free_plan_cache(s->pcache);
     s->stage_ring[s->stage_slot].h = s->h_stage;
     for (int k = 0; k < gpurir_sim::kStageRing; k++)
@@ -590,7 +599,7 @@ static int check_status(gpurir_sim *s) {
 
 // Byte layout of one launch's descriptors (mirrored host staging -> device).
 struct Layout {
-    size_t o_rooms, o_items, o_rirs, o_groups, o_pos, stage_bytes, o_env, o_axis, o_part, o_skip, o_out,
+    size_t o_rooms, o_items, o_rirs, o_groups, o_pos, o_pre, stage_bytes, o_env, o_axis, o_part, o_skip, o_out,
         dev_bytes;
 };
 
@@ -601,7 +610,8 @@ static Layout make_layout(const Plan &P, size_t n_rooms, long n_src, long n_rcv,
     L.o_rooms = 0;
     L.o_pos = align_up(L.o_rooms + n_rooms * sizeof(RoomDesc), 256);
     size_t n_pos = host_io ? (size_t)(n_src + n_rcv) * 3 * 2 : 0;
-    L.o_items = align_up(L.o_pos + n_pos * sizeof(float), 256);
+    L.o_pre = align_up(L.o_pos + n_pos * sizeof(float), 256);   // per-RIR silent-tail flags (host I/O)
+    L.o_items = align_up(L.o_pre + (host_io ? (size_t)M : 0), 256);
     L.o_rirs = align_up(L.o_items + P.items.size() * sizeof(IsmItem), 256);
     L.o_groups = align_up(L.o_rirs + P.rirs.size() * sizeof(IsmItem), 256);
     L.stage_bytes = align_up(L.o_groups + P.groups.size() * sizeof(PartGroup), 256);
@@ -663,7 +673,8 @@ static void fill_stage(char *h, const Layout &L, const std::vector<RoomDesc> &R,
 static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const Layout &L, long M,
                            const float *dps, const float *dpr, const float *dos, const float *dor,
                            float *dout, int *work_counter, const uint64_t *offset_ptr,
-                           cudaStream_t st, bool record, bool skip_ready = false) {
+                           cudaStream_t st, bool record, bool skip_ready = false,
+                           const unsigned char *tail_pre = nullptr) {
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(d + L.o_rooms);
     if (record && s->profile && P.grid > 0) { CK(cudaEventRecord(s->ev[0], st)); s->ev_ism = true; }
     TailArgs ta;
@@ -673,6 +684,7 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     ta.noise_kind = s->noise;
     ta.env_out = reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env);
     ta.fuse = 1;
+    ta.pre = tail_pre;
     if (record) s->last_launches = (P.grid > 0 ? 1 : 0);
     unsigned char *skip = nullptr;
     if (P.grid > 0 && P.skip_flags) {   // segments no image may reach: flags at the current positions
@@ -713,7 +725,8 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
 // store into it, but pages not yet touched fault one by one from the GPU side,
 // far slower than the copy.  GPURIR_HOST_DIRECT=0 turns direct stores off,
 // =2 allows them into pageable memory as well.
-static float *host_output_pointer(gpurir_sim *s, float *out) {
+static float *host_output_pointer(gpurir_sim *s, float *out, bool *pinned = nullptr) {
+    if (pinned) *pinned = false;
     if (s->host_direct < 0) {
         const char *env = getenv("GPURIR_HOST_DIRECT");
         int pageable = 0, host_tables = 0;
@@ -728,9 +741,78 @@ static float *host_output_pointer(gpurir_sim *s, float *out) {
         cudaGetLastError();
         return nullptr;
     }
-    if (pa.type == cudaMemoryTypeHost && pa.devicePointer) return static_cast<float *>(pa.devicePointer);
+    if (pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+        if (pinned) *pinned = true;
+        return static_cast<float *>(pa.devicePointer);
+    }
     if (pa.type == cudaMemoryTypeUnregistered && s->host_direct == 2) return out;
     return nullptr;
+}
+
+// True when the diffuse tail of the RIR (source ps, receiver pr) of room r is certainly
+// silent: its envelope window [w_start, nISM) is empty, or no image of the pair can
+// reach it (then every window sample is an exact zero and A = 0).  Conservative: the
+// window start is taken one sample early, and images_miss_segment keeps a margin.
+static bool tail_silent(const RoomDesc &r, const float *ps, const float *pr) {
+    double d2 = 0.0;
+    for (int a = 0; a < 3; a++) d2 += ((double)ps[a] - pr[a]) * ((double)ps[a] - pr[a]);
+    const double tau_dp = std::sqrt(d2) * ((double)r.kh + r.kl);
+    const double w = std::max((double)r.n_ism - 0.01 * r.fs, tau_dp);
+    if (w - 1.0 >= (double)r.n_ism) return true;
+    return images_miss_segment(r.L, r.nb, ps, pr, r.kh, r.H, (int)std::ceil(w) - 1, r.n_ism);
+}
+
+// Silent tails of a host-output call: flags per RIR into `flags` (the kernel then
+// writes only their envelope) and, on the side stream, one 2-D copy from a device
+// zero buffer per run of consecutive rows, so that those bytes cross the host link
+// while the kernel computes the early parts.  Returns whether any tail was taken.
+static int stream_silent_tails(gpurir_sim *s, const std::vector<RoomDesc> &R, const Plan &P,
+                               const float *pos_src, const float *pos_rcv, float *out, unsigned char *flags,
+                               bool &any) {
+    any = false;
+    const long M = (long)P.rirs.size();
+    memset(flags, 0, (size_t)M);
+    struct Run { long long row; long n; int room; };
+    std::vector<Run> runs;
+    size_t need = 0;
+    for (long m = 0; m < M; m++) {
+        const IsmItem &it = P.rirs[m];
+        const RoomDesc &r = R[it.room];
+        if (it.t_hi != -1 || r.n_total <= r.n_ism) continue;   // tail not fused, or none
+        if (!tail_silent(r, pos_src + 3 * it.src, pos_rcv + 3 * it.rcv)) continue;
+        flags[it.rir] = 1;
+        if (!runs.empty() && runs.back().room == it.room &&
+            runs.back().row + runs.back().n * r.n_total == it.out_row)
+            runs.back().n++;
+        else
+            runs.push_back({it.out_row, 1, it.room});
+        need = std::max(need, (size_t)runs.back().n * (size_t)(r.n_total - r.n_ism) * sizeof(float));
+    }
+    if (runs.empty()) return GPURIR_OK;
+    if (!s->side) {
+        CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&s->side_done, cudaEventDisableTiming));
+    }
+    if (need > s->zero_bytes) {
+        if (s->d_zero) {
+            CK(cudaStreamSynchronize(s->side));
+            CK(cudaFree(s->d_zero));
+            s->d_zero = nullptr;
+            s->zero_bytes = 0;
+        }
+        CK(cudaMalloc(&s->d_zero, need));
+        CK(cudaMemsetAsync(s->d_zero, 0, need, s->side));
+        s->zero_bytes = need;
+    }
+    for (const Run &u : runs) {
+        const RoomDesc &r = R[u.room];
+        const size_t width = (size_t)(r.n_total - r.n_ism) * sizeof(float);
+        CK(cudaMemcpy2DAsync(out + u.row + r.n_ism, (size_t)r.n_total * sizeof(float), s->d_zero, width, width,
+                             (size_t)u.n, cudaMemcpyDeviceToHost, s->side));
+    }
+    CK(cudaEventRecord(s->side_done, s->side));
+    any = true;
+    return GPURIR_OK;
 }
 
 // Shared body of the single-room and batched entry points, host or device I/O.
@@ -765,6 +847,22 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     else fill_stage(h, L, R, P);
     const float *dps = pos_src, *dpr = pos_rcv, *dos = orV_src, *dor = orV_rcv;
     char *d = s->d_ws;
+    // Host output the GPU can store to directly (pinned memory, or any host memory on
+    // systems whose GPU shares the CPU's page tables, e.g. over NVLink-C2C): the kernels
+    // write the RIRs there during compute and no device->host copy follows.
+    bool direct = false, pinned = false;
+    float *hout = nullptr;
+    if (host_io) {
+        hout = host_output_pointer(s, out, &pinned);
+        direct = hout != nullptr;
+    }
+    // ... and, into page-locked memory, tails silent by geometry are streamed by a copy
+    // engine meanwhile
+    bool pre = false;
+    if (host_io && pinned && P.grid > 0 && P.max_n_diff > 0)
+        if ((rc = stream_silent_tails(s, R, P, pos_src, pos_rcv, out,
+                                      reinterpret_cast<unsigned char *>(h + L.o_pre), pre)))
+            return rc;
     if (host_io) {
         float *hp = reinterpret_cast<float *>(h + L.o_pos);
         memcpy(hp, pos_src, sizeof(float) * 3 * n_src);
@@ -782,21 +880,15 @@ static int simulate_rooms(gpurir_sim *s, std::vector<RoomDesc> &R, long n_src, l
     s->stage_pending = true;
     if (!items_resident) s->pcache->gen = ++s->ws_gen;
     if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(d + L.o_rooms), (int)R.size(), d_beta, st));
-    float *dout = host_io ? reinterpret_cast<float *>(d + L.o_out) : out;
-    // Host output the GPU can store to directly (pinned memory, or any host memory on
-    // systems whose GPU shares the CPU's page tables, e.g. over NVLink-C2C): the kernels
-    // write the RIRs there during compute and no device->host copy follows.
-    bool direct = false;
-    if (host_io) {
-        float *hp = host_output_pointer(s, out);
-        if (hp) { dout = hp; direct = true; }
-    }
+    float *dout = host_io ? (direct ? hout : reinterpret_cast<float *>(d + L.o_out)) : out;
     s->last_direct = direct;
     s->ev_ism = s->ev_tail = false;
     s->last_h2d = up_bytes;
     s->last_d2h = sizeof(int) + (host_io ? (uint64_t)out_elems * sizeof(float) : 0);
-    if ((rc = enqueue_kernels(s, P, d, L, M, dps, dpr, dos, dor, dout, s->d_ctl, nullptr, st, true)))
+    if ((rc = enqueue_kernels(s, P, d, L, M, dps, dpr, dos, dor, dout, s->d_ctl, nullptr, st, true, false,
+                              pre ? reinterpret_cast<const unsigned char *>(d + L.o_pre) : nullptr)))
         return rc;
+    if (pre) CK(cudaStreamWaitEvent(st, s->side_done, 0));   // the call ends after the streamed tails
     s->env_off = L.o_env;
     s->last_n_rir = P.max_n_diff > 0 ? M : 0;
     s->calls++;

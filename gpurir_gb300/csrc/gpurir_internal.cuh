@@ -206,7 +206,8 @@ __device__ __forceinline__ void image_axis(int n, int N, int &clust, int &refl) 
 // k L + s for even k and (k + 1) L - s for odd k: each parity is increasing in k, so
 // its extremes are at its first and last index and it crosses zero at most once.
 // Plain FP32 (a bound to a few 1e-6 relative; callers leave a margin).
-__device__ __forceinline__ void axis_extent(int N, float L, float s, float r, float &v2min, float &v2max) {
+__host__ __device__ __forceinline__ void axis_extent(int N, float L, float s, float r, float &v2min,
+                                                    float &v2max) {
     const int k_min = -(N / 2), k_max = N - 1 - N / 2;
     v2min = 3.0e38f;
     v2max = 0.0f;
@@ -225,9 +226,9 @@ __device__ __forceinline__ void axis_extent(int N, float L, float s, float r, fl
 // True when no image of the pair (src, rcv) has a delay within reach of the samples
 // [t_lo, t_hi): every delay lies below t_lo - H - margin or above t_hi + H + margin.
 // fs_c = Fs / c in samples per metre.
-__device__ __forceinline__ bool images_miss_segment(const float L[3], const int nb[3], const float s[3],
-                                                    const float r[3], float fs_c, float H, int t_lo,
-                                                    int t_hi) {
+__host__ __device__ __forceinline__ bool images_miss_segment(const float L[3], const int nb[3],
+                                                             const float s[3], const float r[3], float fs_c,
+                                                             float H, int t_lo, int t_hi) {
     float lo2 = 0.0f, hi2 = 0.0f;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -313,6 +314,9 @@ struct TailArgs {
     int noise_kind;
     float *env_out;               // optional [rir][3]: A, alpha, tau_dp
     int fuse;
+    // optional [rir]: 1 = the RIR's tail is silent and written by someone else (a copy
+    // engine streaming zeros into host memory); the kernel writes only its envelope
+    const unsigned char *pre = nullptr;
 };
 
 // Error codes shared by kernels and host (written to a device status word).

@@ -70,6 +70,7 @@ struct IsmLaunch {
     int axis_cap;
     float *partial;   // partial segments of items holding a part of an RIR's images
     const unsigned char *skip;   // per item: 1 = no image reaches its segment (nullptr: none)
+    const unsigned char *tail_pre;   // per RIR: 1 = silent tail written elsewhere (TailArgs::pre)
 };
 
 // Evaluation modes of the taps (template parameter MODE):
@@ -362,7 +363,16 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
         // earlier items' stores already keep the link busy (mic_array into host memory:
         // 0.79 ms instead of 0.83 ms; no change into HBM).
         bool tail_written = false;
-        if (fuse && item_id < (int)gridDim.x) {
+        if (fuse && P.tail_pre && P.tail_pre[it.rir]) {
+            // the caller streams this silent tail itself: only its envelope (A = 0) here
+            const TailEnv e = tail_envelope(R, 0.0f, w_start, tau_dp);
+            if (tid == 0 && P.env_out) {
+                P.env_out[3 * it.rir] = e.A;
+                P.env_out[3 * it.rir + 1] = e.alpha;
+                P.env_out[3 * it.rir + 2] = tau_dp;
+            }
+            tail_written = true;
+        } else if (fuse && item_id < (int)gridDim.x) {
             const float s3[3] = {sx, sy, sz}, r3[3] = {rx, ry, rz};
             if (images_miss_segment(R.L, R.nb, s3, r3, R.kh, H, w_start, R.n_ism)) {
                 const TailEnv e = tail_envelope(R, 0.0f, w_start, tau_dp);
@@ -874,6 +884,7 @@ cudaError_t ism_forward_launch(int tpl, const RoomDesc *rooms, const IsmItem *it
     p.noise_kind = tail ? tail->noise_kind : 0;
     p.env_out = tail ? tail->env_out : nullptr;
     p.fuse_tail = tail ? tail->fuse : 0;
+    p.tail_pre = tail ? tail->pre : nullptr;
     p.rooms = rooms; p.items = items; p.n_items = n_items;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.orv_src = orv_src; p.orv_rcv = orv_rcv;
     p.out = out; p.work_counter = work_counter; p.status = status;
