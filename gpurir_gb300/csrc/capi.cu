@@ -772,6 +772,34 @@ static int stream_silent_tails(gpurir_sim *s, const std::vector<RoomDesc> &R, co
     any = false;
     const long M = (long)P.rirs.size();
     memset(flags, 0, (size_t)M);
+    // Per room first: with every source and receiver inside the room, an image lies
+    // within (N/2 + 1) L of the receiver on each axis, and every window starts at
+    // nISM - 10 ms or later; when even that farthest delay stays clear of the earliest
+    // window, all the room's tails are silent without a test per pair.
+    std::vector<char> room_silent(R.size(), 0);
+    for (size_t k = 0; k < R.size(); k++) {
+        const RoomDesc &r = R[k];
+        bool inside = true;
+        for (int i = 0; i < r.n_src && inside; i++)
+            for (int a = 0; a < 3; a++) {
+                const float v = pos_src[3 * (r.src_off + i) + a];
+                inside &= v >= 0.0f && v <= r.L[a];
+            }
+        for (int i = 0; i < r.n_rcv && inside; i++)
+            for (int a = 0; a < 3; a++) {
+                const float v = pos_rcv[3 * (r.rcv_off + i) + a];
+                inside &= v >= 0.0f && v <= r.L[a];
+            }
+        if (!inside) continue;
+        double reach2 = 0.0;
+        for (int a = 0; a < 3; a++) {
+            const double e = (double)(r.nb[a] / 2 + 1) * r.L[a];
+            reach2 += e * e;
+        }
+        const double tau_hi = std::sqrt(reach2) * ((double)r.kh + r.kl);
+        const double w_min = (double)r.n_ism - 0.01 * r.fs - 1.0;
+        room_silent[k] = tau_hi < w_min - r.H - 2.0 - 1e-5 * tau_hi;
+    }
     struct Run { long long row; long n; int room; };
     std::vector<Run> runs;
     size_t need = 0;
@@ -779,7 +807,7 @@ static int stream_silent_tails(gpurir_sim *s, const std::vector<RoomDesc> &R, co
         const IsmItem &it = P.rirs[m];
         const RoomDesc &r = R[it.room];
         if (it.t_hi != -1 || r.n_total <= r.n_ism) continue;   // tail not fused, or none
-        if (!tail_silent(r, pos_src + 3 * it.src, pos_rcv + 3 * it.rcv)) continue;
+        if (!room_silent[it.room] && !tail_silent(r, pos_src + 3 * it.src, pos_rcv + 3 * it.rcv)) continue;
         flags[it.rir] = 1;
         if (!runs.empty() && runs.back().room == it.room &&
             runs.back().row + runs.back().n * r.n_total == it.out_row)

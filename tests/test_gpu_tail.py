@@ -96,22 +96,26 @@ def test_empty_envelope_window_gives_silent_tail(built):
     assert np.all(out[..., 16:] == 0)
 
 
-def test_silent_tails_of_every_wave_match_the_oracle(built):
+@pytest.mark.parametrize("tdiff", [0.3, 0.21])
+def test_silent_tails_of_every_wave_match_the_oracle(built, tdiff):
     """More RIRs than the persistent grid holds, every tail silent by geometry (no image
-    reaches the envelope window): the first wave of items writes its tails before the
-    taps, later items after them; both give the oracle's envelope (A = 0) and zeros, and
-    repeated calls are bitwise equal."""
+    reaches the envelope window).  Into page-locked memory the call streams such tails
+    by a copy engine (at Tdiff 0.3 s the room-wide bound proves them silent, at 0.21 s
+    only the bound per pair can); the first wave of items would write them before the
+    taps, later items after.  Every path gives the oracle's envelope (A = 0) and zeros,
+    and repeated calls are bitwise equal."""
     import gpurir_gb300 as G
     rng = np.random.default_rng(13)
     room = [6.0, 5.0, 3.0]
     beta = G.beta_SabineEstimation(room, 1.0)
     ps = _rand_inside(rng, 32, room, 0.5)   # 640 RIRs: one item each, about two waves
-    pr = _rand_inside(rng, 20, room, 0.5)
-    nb, tdiff, tmax, fs = [12, 14, 24], 0.3, 0.6, 16000.0
+    v = rng.standard_normal((20, 3))        # receivers on a 0.2 m sphere at the centre
+    pr = (np.asarray(room) / 2 + 0.2 * v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    nb, tmax, fs = [12, 14, 24], 0.6, 16000.0
     sim = G.Simulator(seed=21)
     sim.set_noise("gaussian")
     a = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, tdiff, tmax, fs).copy()
-    assert sim.last_launch_count() == 1   # tails written by the ISM kernel itself
+    assert sim.last_launch_count() == 1   # no separate tail kernel
     env = sim.last_envelope(ps.shape[0] * pr.shape[0])
     b = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, tdiff, tmax, fs)
     assert np.array_equal(a, b)
@@ -124,3 +128,35 @@ def test_silent_tails_of_every_wave_match_the_oracle(built):
     assert np.allclose(env[:, 2], p["tau_dp"].ravel(), rtol=1e-6)
     assert np.all(a[..., n_ism:] == 0)
     assert rel_l2(a[..., :n_ism], ref[..., :n_ism]) < 1e-6
+
+
+def test_silent_and_live_tails_mixed(built):
+    """Receivers spread over the room at Tdiff 0.195 s: about half of the 640 tails carry
+    energy and the others are silent, so the streamed silent tails come in many short
+    runs of rows between live ones.  Envelopes and tails match the oracle fed the same
+    Philox stream."""
+    import gpurir_gb300 as G
+    rng = np.random.default_rng(13)
+    room = [6.0, 5.0, 3.0]
+    beta = G.beta_SabineEstimation(room, 1.0)
+    ps = _rand_inside(rng, 32, room, 0.5)
+    rng.standard_normal((20, 3))
+    pr = _rand_inside(rng, 20, room, 0.5)
+    nb, tdiff, tmax, fs = [12, 14, 24], 0.195, 0.6, 16000.0
+    sim = G.Simulator(seed=23)
+    sim.set_noise("gaussian")
+    out = sim.simulate_rir(room, beta, ps, pr, None, None, 0, 0, nb, tdiff, tmax, fs)
+    env = sim.last_envelope(ps.shape[0] * pr.shape[0])
+    ref, p = oracle.simulate_rir(room, beta, ps, pr, nb, tmax, fs, Tdiff=tdiff, seed=23, offset=0,
+                                 noise="gaussian", return_parts=True)
+    n_ism = p["n_ism"]
+    live = p["A"].ravel() > 0
+    assert 0 < live.sum() < live.size
+    assert np.array_equal(env[:, 0] > 0, live)
+    assert rel_l2(env[live, 0], p["A"].ravel()[live]) < 1e-4
+    assert np.allclose(env[:, 1], p["alpha"].ravel(), rtol=1e-6)
+    assert np.allclose(env[:, 2], p["tau_dp"].ravel(), rtol=1e-6)
+    tails, rtails = out[..., n_ism:].reshape(-1, out.shape[-1] - n_ism), ref[..., n_ism:].reshape(live.size, -1)
+    assert np.all(tails[~live] == 0)
+    assert rel_l2(tails[live], rtails[live]) < 1e-4
+    assert rel_l2(out[..., :n_ism], ref[..., :n_ism]) < 1e-6
