@@ -3,8 +3,11 @@
 Every RIR depends only on its room, source and receiver, so a multi-GPU run has
 no exchange on the data path: rooms are dealt to ranks by estimated cost
 (longest first, each to the least-loaded rank), every rank simulates its rooms
-with one batched launch, and the results are gathered on the host.  The only
-collectives are this gather and the max-over-ranks of a time.
+with one batched launch, and the results are gathered on the host.  A moving-source
+trajectory is dealt by contiguous runs of its points: each rank filters its run, and
+adjacent runs overlap only in the L - 1 samples past a run's end, which the host
+gather adds up.  The only collectives are these gathers and the max-over-ranks of a
+time.
 """
 import math
 
@@ -62,6 +65,48 @@ def simulate_sharded(rooms, fs, simulate=None, group=None):
         for i, arr in piece:
             result[i] = arr
     return result
+
+
+def trajectory_shards(n_pts, world):
+    """Contiguous runs of trajectory points [p0, p1) per rank, as equal as the count
+    allows (every point costs one convolution per receiver)."""
+    bounds = [n_pts * k // world for k in range(world + 1)]
+    return [(bounds[k], bounds[k + 1]) for k in range(world)]
+
+
+def _gpu_trajectory(source_signal, RIRs, timestamps, fs):
+    from .trajectory import simulate_trajectory
+    return simulate_trajectory(source_signal, RIRs, timestamps, fs)
+
+
+def simulate_trajectory_sharded(source_signal, RIRs, timestamps=None, fs=None, simulate=None, group=None):
+    """simulateTrajectory (float64 [len(signal) + L - 1, R]) over the ranks of `group`
+    (torch.distributed, initialised).  Rank k filters the points of its run [p0, p1):
+    its slice of the signal, cut at the same samples as the whole call cuts it, with
+    those points' RIRs, by `simulate(signal, RIRs, timestamps, fs)` (default: the GPU
+    call); every rank returns the sum of all runs placed at their first samples."""
+    import torch.distributed as dist
+    from .trajectory import segment_bounds
+    simulate = simulate or _gpu_trajectory
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    sig = np.asarray(source_signal)
+    P, R, L = RIRs.shape
+    w_ini = segment_bounds(len(sig), P, timestamps, fs)
+    p0, p1 = trajectory_shards(P, world)[rank]
+    piece = None
+    if p1 > p0:
+        # timestamps in samples (fs = 1): the run's cut points exactly
+        local = simulate(sig[w_ini[p0]:w_ini[p1]], RIRs[p0:p1],
+                         (w_ini[p0:p1] - w_ini[p0]).astype(np.float64), 1.0)
+        piece = (int(w_ini[p0]), np.asarray(local, dtype=np.float64))
+    pieces = [None] * world
+    dist.all_gather_object(pieces, piece, group=group)
+    out = np.zeros((len(sig) + L - 1, R), dtype=np.float64)
+    for pc in pieces:
+        if pc is not None:
+            off, a = pc
+            out[off:off + a.shape[0]] += a
+    return out
 
 
 def max_over_ranks(value, group=None):

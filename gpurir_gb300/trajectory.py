@@ -9,18 +9,24 @@ hand-written FFT kernels behind the C ABI (gpurir_trajectory_*).
 import numpy as np
 
 
+def segment_bounds(n, n_pts, timestamps=None, fs=None):
+    """First sample of every segment and the signal length, w_ini int [n_pts + 1], as
+    gpuRIR/__init__.py:198-205 forms them."""
+    assert timestamps is None or fs is not None, "fs must be indicated for custom timestamps"
+    assert timestamps is None or timestamps[0] == 0, "The first timestamp must be 0"
+    if timestamps is None:
+        fs = n / n_pts
+        timestamps = np.arange(n_pts)
+    return np.append((np.asarray(timestamps) * fs).astype(int), n)
+
+
 def segment_signal(source_signal, n_pts, timestamps=None, fs=None):
     """Segmentation of gpuRIR/__init__.py:198-213.
 
     Returns (segments float32 [n_pts, max_len], w_ini int [n_pts + 1], w_len int [n_pts]).
     """
     n = len(source_signal)
-    assert timestamps is None or fs is not None, "fs must be indicated for custom timestamps"
-    assert timestamps is None or timestamps[0] == 0, "The first timestamp must be 0"
-    if timestamps is None:
-        fs = n / n_pts
-        timestamps = np.arange(n_pts)
-    w_ini = np.append((np.asarray(timestamps) * fs).astype(int), n)
+    w_ini = segment_bounds(n, n_pts, timestamps, fs)
     w_len = np.diff(w_ini)
     width = int(w_len.max())
     sig = np.asarray(source_signal)

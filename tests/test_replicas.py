@@ -78,3 +78,61 @@ def test_two_gloo_ranks_gather_every_room(tmp_path):
         assert float(z["t"]) == 2.5
         for i, w in enumerate(want):
             assert np.array_equal(z["r%d" % i], w)
+
+
+def _traj_case(custom):
+    rng = np.random.default_rng(6)
+    sig = rng.standard_normal(3001).astype(np.float32)
+    rirs = (0.1 * rng.standard_normal((9, 2, 50))).astype(np.float32)
+    if not custom:
+        return sig, rirs, None, None
+    # uneven segments, timestamps in seconds at 10 kHz
+    ts = np.array([0.0, 0.013, 0.05, 0.061, 0.1, 0.17, 0.2, 0.23, 0.29])
+    return sig, rirs, ts, 10000.0
+
+
+def _oracle_trajectory(sig, rirs, ts, fs):
+    import oracle
+    return oracle.trajectory(sig, rirs, ts, fs)
+
+
+def _traj_worker(rank, world, port, out_dir):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        for custom in (False, True):
+            sig, rirs, ts, fs = _traj_case(custom)
+            res = replicas.simulate_trajectory_sharded(sig, rirs, ts, fs, simulate=_oracle_trajectory)
+            np.save(os.path.join(out_dir, "traj%d_%d.npy" % (rank, custom)), res)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_trajectory_shards_are_contiguous_runs():
+    for n_pts, world in [(9, 2), (400, 8), (2, 3), (1, 1)]:
+        runs = replicas.trajectory_shards(n_pts, world)
+        assert len(runs) == world and runs[0][0] == 0 and runs[-1][1] == n_pts
+        assert all(a[1] == b[0] for a, b in zip(runs, runs[1:]))
+        sizes = [p1 - p0 for p0, p1 in runs]
+        assert max(sizes) - min(sizes) <= 1
+
+
+def test_two_gloo_ranks_overlap_add_a_trajectory(tmp_path):
+    """Each rank filters a contiguous run of trajectory points (the oracle standing in for
+    the GPU call); the gathered runs, overlapping in L - 1 samples at the run edge, equal
+    the unsharded overlap-add, with equal and with custom segments."""
+    import oracle
+    import torch.multiprocessing as mp
+    world = 2
+    mp.start_processes(_traj_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world,
+                       start_method="spawn", join=True)
+    for custom in (False, True):
+        sig, rirs, ts, fs = _traj_case(custom)
+        want = oracle.trajectory(sig, rirs, ts, fs)
+        for rank in range(world):
+            got = np.load(tmp_path / ("traj%d_%d.npy" % (rank, custom)))
+            assert got.shape == want.shape
+            assert np.allclose(got, want, rtol=1e-12, atol=1e-12)
