@@ -50,8 +50,9 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the batched / adjoint / trajectory measurements")
-    p.add_argument("--extras", default="batched,inverse,trajectory,tuning",
-                   help="comma list of the extra measurements to run (batched, inverse, trajectory, tuning)")
+    p.add_argument("--extras", default="batched,inverse,trajectory,tuning,modes",
+                   help="comma list of the extra measurements to run (batched, inverse, trajectory, tuning, "
+                        "modes)")
     return p.parse_args()
 
 
@@ -231,7 +232,7 @@ def _timed(fn, steps, stream, flush=None):
     return ts[len(ts) // 2]
 
 
-def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory", "tuning")):
+def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory", "tuning", "modes")):
     """The metric's other parts: batched vs plain forward (512 uneven rooms), forward +
     adjoint step vs forward (16 rooms x 32 RIRs), trajectory filtering (400 points)."""
     import torch
@@ -248,7 +249,44 @@ def run_extras(G, flush, stream, which=("batched", "inverse", "trajectory", "tun
         out.update(_extra_trajectory(workloads, sim, flush, stream, fs, dev))
     if "tuning" in which:
         out.update(_extra_tuning(G, B, workloads, flush, stream, fs, dev))
+    if "modes" in which:
+        out.update(_extra_modes(G, workloads, flush, stream, dev))
     return out
+
+
+def _extra_modes(G, workloads, flush, stream, dev):
+    """The main workload (mic_array) in gpuRIR's two other evaluation modes, mixed
+    precision and lookup table: kernel time and the error of the timed output against
+    the FP64 oracle, as for the FP32 line."""
+    import torch
+    scene = workloads.mic_array()
+    sp, mp = G.polar_patterns[scene["spkr_pattern"]], G.polar_patterns[scene["mic_pattern"]]
+    ms, mr = scene["pos_src"].shape[0], scene["pos_rcv"].shape[0]
+    ns = workloads.n_samples(scene["Tmax"], scene["fs"])
+    d_ps = torch.from_numpy(scene["pos_src"]).to(dev)
+    d_pr = torch.from_numpy(scene["pos_rcv"]).to(dev)
+    d_or = torch.from_numpy(scene["orV_rcv"]).to(dev)
+    d_out = torch.empty((ms, mr, ns), dtype=torch.float32, device=dev)
+    res = {}
+    for name in ("mixed_precision", "lut"):
+        sim = G.Simulator(mixed_precision=name == "mixed_precision", lut=name == "lut", seed=1234)
+        sim.set_noise(scene["noise"])
+
+        def step():
+            sim.simulate_rir_device(scene["room_sz"], scene["beta"], d_ps, d_pr, None, d_or, sp, mp,
+                                    scene["nb_img"], scene["Tdiff"], scene["Tmax"], scene["fs"],
+                                    scene["c"], d_out, stream.cuda_stream)
+
+        for _ in range(3):
+            step()
+        t = _timed(step, 20, stream, flush)
+        seed_used, calls_after = sim.get_seed()
+        acc = _accuracy(G, scene, d_out, seed_used, calls_after - 1)
+        res[name] = {"ms_per_step": t, "rirs_per_s": ms * mr / (t * 1e-3), "accuracy": acc["early"],
+                     "rirs_checked": acc["rirs_checked"]}
+    return {"modes": dict(res, note="mic_array in each mode, device-resident, L2 flushed; accuracy of the "
+                                    "early part of 64 timed RIRs against the FP64 oracle (exact sinc "
+                                    "sum); FP32 is the main line")}
 
 
 def _extra_tuning(G, B, workloads, flush, stream, fs, dev):
