@@ -448,6 +448,17 @@ static int plan_window(float H, Plan &P, int &max_nsub) {
     return GPURIR_OK;
 }
 
+// Latest sample any image of the room can reach while source and receiver are inside
+// it: |receiver -> image| <= (N/2 + 1) L per axis, plus the window and a margin.
+static double room_span(const RoomDesc &r) {
+    double reach2 = 0.0;
+    for (int a = 0; a < 3; a++) {
+        const double e = (double)(r.nb[a] / 2 + 1) * r.L[a];
+        reach2 += e * e;
+    }
+    return std::sqrt(reach2) * ((double)r.kh + r.kl) + r.H + 2.0;
+}
+
 // Work items for a set of rooms.  Every RIR is cut into segments of at most
 // what one block's shared memory holds; RIRs of small launches are cut finer so
 // that the persistent grid has work for every SM.  Items are ordered by an
@@ -496,12 +507,7 @@ static int plan_rooms(gpurir_sim *s, const std::vector<RoomDesc> &R, Plan &P) {
         // |receiver -> image| <= (N/2 + 1) L per axis.  Only an estimate for the cost
         // order (segments beyond it hold no image); the kernels test each item against
         // the actual positions and skip the image work of segments no image reaches.
-        double reach2 = 0.0;
-        for (int a = 0; a < 3; a++) {
-            const double e = (double)(r.nb[a] / 2 + 1) * r.L[a];
-            reach2 += e * e;
-        }
-        const double span = std::sqrt(reach2) * ((double)r.kh + r.kl) + r.H + 2.0;
+        const double span = room_span(r);
         auto cut = [&](long lo, long hi, long n) {   // n segments of [lo, hi), 32-aligned
             const long t = std::min<long>(align_up((size_t)((hi - lo + n - 1) / n), 32), seg_max);
             for (long a = lo; a < hi; a += t) segs.push_back({(int)a, (int)std::min(a + t, hi)});
@@ -1246,6 +1252,40 @@ static void csr(const std::vector<IsmItem> &items, int n_target, int IsmItem::*f
     for (size_t i = 0; i < items.size(); i++) list[fill[items[i].*field - base_sub]++] = (int)i;
 }
 
+// Adjoint work items: the forward's, in the same order, except that the items of an
+// incomplete last wave of G blocks (all of them when there is only one) are cut by
+// images into up to 8 parts, as many as fill the wave.  The adjoint's items of one
+// batch cost about the same, so whole items would leave that wave mostly idle; the
+// parts fill it (each part restages its segment of dL/dh, which is why the full waves
+// stay whole).  On the inverse problem (512 items, 456 blocks) the adjoint takes ~66 us
+// instead of ~76 us; cutting every item in two gave ~70 us, in three ~78 us.  Items past
+// every image's delay stay whole (they only test and leave) and go last.
+static std::vector<IsmItem> adjoint_items(const Plan &P, const std::vector<RoomDesc> &R, long G) {
+    G = std::max<long>(G, 1);
+    std::vector<IsmItem> real, bitems, empties;
+    for (const IsmItem &it : P.items) {
+        const bool empty = it.t_lo > 0 && it.t_lo >= room_span(R[it.room]);
+        (empty ? empties : real).push_back(it);
+    }
+    const long n_real = (long)real.size();
+    const long rem = n_real % G;   // items of the last, incomplete wave
+    for (long i = 0; i < n_real; i++) {
+        const IsmItem &it = real[i];
+        const int n = it.i_hi - it.i_lo;
+        int parts = 1;
+        if (rem > 0 && i >= n_real - rem) parts = (int)std::max<long>(2, std::min<long>(8, G / rem));
+        parts = std::min(parts, std::max(n, 1));
+        for (int k = 0; k < parts; k++) {
+            IsmItem h = it;
+            h.i_lo = it.i_lo + (int)((long long)n * k / parts);
+            h.i_hi = it.i_lo + (int)((long long)n * (k + 1) / parts);
+            bitems.push_back(h);
+        }
+    }
+    bitems.insert(bitems.end(), empties.begin(), empties.end());
+    return bitems;
+}
+
 static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, float Fs, float c,
                           const float *d_beta, const float *d_pos_src, const float *d_pos_rcv,
                           const float *d_orV_src, const float *d_orV_rcv, const float *d_grad_rir,
@@ -1305,9 +1345,10 @@ static int backward_batch(gpurir_sim *s, int n_rooms, const gpurir_room *rooms, 
         if (smem > 227 * 1024) return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
         bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, smem);
         if (bps < 1) return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
-        if (tuning(2) > 0) bps = std::min(bps, tuning(2));   // adjoint_blocks_per_sm (tuning.cu)
     }
-    const std::vector<IsmItem> &bi = P.items;
+    // work items split as the training batch splits them (gpurir_adjoint_create)
+    const std::vector<IsmItem> bi = adjoint_items(P, R, (long)s->num_sms * bps);
+    if (!P.items.empty() && tuning(2) > 0) bps = std::min(bps, tuning(2));   // adjoint_blocks_per_sm (tuning.cu)
     const int n_items = (int)bi.size();
     std::vector<int> p_room, l_room, p_src, l_src, p_rcv, l_rcv;
     csr(bi, n_rooms, &IsmItem::room, 0, p_room, l_room);
@@ -1372,7 +1413,8 @@ struct gpurir_adjoint {
     int max_tseg = 1, grid_b = 0;
     bool need_orv_src = false, need_orv_rcv = false;
     bool rooms_written = false;   // a forward call has written the room tables
-    size_t o_arr[6] = {}, o_ig = 0, o_ctl = 0;
+    size_t o_arr[6] = {}, o_ig = 0, o_bitems = 0, o_ctl = 0;
+    int n_bitems = 0;             // adjoint work items (the forward's, split; see gpurir_adjoint_create)
     float *d_g = nullptr;         // dL/dRIR of the fused L2 step (allocated by its first call)
     double *d_partial = nullptr;  // per-block partial sums of the loss
 };
@@ -1410,7 +1452,7 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
         delete a;
         return fail(GPURIR_ERR_UNSUPPORTED, "segment too long for the adjoint");
     }
-    int bps = 0;
+    int bps = 0, bps_occ = 0;
     if (!P.items.empty()) {
         bps = ism_backward_blocks_per_sm(P.tpl, P.clamp, ism_backward_smem_bytes(P.tpl, a->max_tseg, 64 * P.tpl,
                                                                                 P.axis_cap));
@@ -1418,23 +1460,30 @@ extern "C" int gpurir_adjoint_create(gpurir_sim *s, int n_rooms, const gpurir_ro
             delete a;
             return fail(GPURIR_ERR_CUDA, "adjoint kernel does not fit on an SM");
         }
+        bps_occ = bps;
         if (tuning(2) > 0) bps = std::min(bps, tuning(2));   // adjoint_blocks_per_sm (tuning.cu)
     }
-    const int n_items = (int)P.items.size();
+    // (the wave of the occupancy limit, not of a tuned grid: the items, and so the bits
+    // of the gradients, do not depend on the launch-shape knob)
+    const std::vector<IsmItem> bitems = adjoint_items(P, R, (long)s->num_sms * bps_occ);
+    const int n_items = (int)bitems.size();
+    a->n_bitems = n_items;
     a->grid_b = std::min(n_items, s->num_sms * bps);
     std::vector<int> lists[6];
-    csr(P.items, n_rooms, &IsmItem::room, 0, lists[0], lists[1]);
-    csr(P.items, (int)a->ns, &IsmItem::src, 0, lists[2], lists[3]);
-    csr(P.items, (int)a->nr, &IsmItem::rcv, 0, lists[4], lists[5]);
+    csr(bitems, n_rooms, &IsmItem::room, 0, lists[0], lists[1]);
+    csr(bitems, (int)a->ns, &IsmItem::src, 0, lists[2], lists[3]);
+    csr(bitems, (int)a->nr, &IsmItem::rcv, 0, lists[4], lists[5]);
     size_t off = align_up(a->L.o_out, 256);
     for (int k = 0; k < 6; k++) { a->o_arr[k] = off; off = align_up(off + lists[k].size() * sizeof(int), 256); }
     a->o_ig = off;
-    a->o_ctl = align_up(a->o_ig + (size_t)std::max(n_items, 1) * 18 * sizeof(float), 256);
+    a->o_bitems = align_up(a->o_ig + (size_t)std::max(n_items, 1) * 18 * sizeof(float), 256);
+    a->o_ctl = align_up(a->o_bitems + bitems.size() * sizeof(IsmItem), 256);
     const size_t bytes = a->o_ctl + 256;   // [0] forward counter, [1] adjoint counter, [2] status, +16 call offset
     std::vector<char> h(a->o_ctl + 256, 0);
     fill_stage(h.data(), a->L, R, P);
     for (int k = 0; k < 6; k++)
         if (!lists[k].empty()) memcpy(h.data() + a->o_arr[k], lists[k].data(), lists[k].size() * sizeof(int));
+    if (!bitems.empty()) memcpy(h.data() + a->o_bitems, bitems.data(), bitems.size() * sizeof(IsmItem));
     const uint64_t start = s->calls;
     memcpy(h.data() + a->o_ctl + 16, &start, sizeof(start));
     cudaError_t e = cudaMalloc(&a->d, bytes);
@@ -1484,14 +1533,14 @@ extern "C" int gpurir_adjoint_backward(gpurir_adjoint *a, const float *d_beta, c
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     int *ctl = reinterpret_cast<int *>(a->d + a->o_ctl);
     const Plan &P = a->P;
-    const int n_items = (int)P.items.size();
+    const int n_items = a->n_bitems;
     float *ig = reinterpret_cast<float *>(a->d + a->o_ig);
     const RoomDesc *drooms = reinterpret_cast<const RoomDesc *>(a->d + a->L.o_rooms);
     if (d_beta) CK(room_beta_launch(reinterpret_cast<RoomDesc *>(a->d + a->L.o_rooms), a->n_rooms, d_beta, st));
     if (n_items == 0) {
         CK(cudaMemsetAsync(ig, 0, 18 * sizeof(float), st));
     } else {
-        CK(ism_backward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(a->d + a->L.o_items), n_items,
+        CK(ism_backward_launch(P.tpl, drooms, reinterpret_cast<const IsmItem *>(a->d + a->o_bitems), n_items,
                                d_pos_src, d_pos_rcv, d_orV_src, d_orV_rcv, d_grad_rir, ig, ctl + 1, ctl + 2,
                                a->max_tseg, P.axis_cap, a->grid_b, P.clamp, st));
     }
