@@ -36,7 +36,7 @@ cudaError_t partial_reduce_launch(const PartGroup *groups, int n_groups, int max
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
-                        cudaStream_t st);
+                        cudaStream_t st, const unsigned char *pre);
 cudaError_t philox_stream_launch(uint32_t *out, long n, uint64_t seed, uint64_t offset,
                                  uint32_t rir, cudaStream_t st);
 cudaError_t probe_peaks(double *fp32_flops, double *mufu_ops, cudaStream_t st);
@@ -719,7 +719,7 @@ static int enqueue_kernels(gpurir_sim *s, const Plan &P, const char *d, const La
     if (tail_kernel)
         CK(tail_launch(drooms, reinterpret_cast<const IsmItem *>(d + L.o_rirs), (int)M, P.max_n_diff,
                        dps, dpr, dout, s->seed, s->calls, offset_ptr, s->noise,
-                       reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env), st));
+                       reinterpret_cast<float *>(const_cast<char *>(d) + L.o_env), st, tail_pre));
     if (record && s->ev_tail) CK(cudaEventRecord(s->ev[3], st));
     return GPURIR_OK;
 }
@@ -768,10 +768,11 @@ static bool tail_silent(const RoomDesc &r, const float *ps, const float *pr) {
     return images_miss_segment(r.L, r.nb, ps, pr, r.kh, r.H, (int)std::ceil(w) - 1, r.n_ism);
 }
 
-// Silent tails of a host-output call: flags per RIR into `flags` (the kernel then
-// writes only their envelope) and, on the side stream, one 2-D copy from a device
-// zero buffer per run of consecutive rows, so that those bytes cross the host link
-// while the kernel computes the early parts.  Returns whether any tail was taken.
+// Silent tails of a host-output call: flags per RIR into `flags` (the ISM kernel's
+// epilogue, or the tail kernel for RIRs cut into segments, then writes only their
+// envelope) and, on the side stream, one 2-D copy from a device zero buffer per run of
+// consecutive rows, so that those bytes cross the host link while the ISM kernel
+// computes the early parts.  Returns whether any tail was taken.
 static int stream_silent_tails(gpurir_sim *s, const std::vector<RoomDesc> &R, const Plan &P,
                                const float *pos_src, const float *pos_rcv, float *out, unsigned char *flags,
                                bool &any) {
@@ -812,7 +813,7 @@ static int stream_silent_tails(gpurir_sim *s, const std::vector<RoomDesc> &R, co
     for (long m = 0; m < M; m++) {
         const IsmItem &it = P.rirs[m];
         const RoomDesc &r = R[it.room];
-        if (it.t_hi != -1 || r.n_total <= r.n_ism) continue;   // tail not fused, or none
+        if (r.n_total <= r.n_ism) continue;   // no tail
         if (!room_silent[it.room] && !tail_silent(r, pos_src + 3 * it.src, pos_rcv + 3 * it.rcv)) continue;
         flags[it.rir] = 1;
         if (!runs.empty() && runs.back().room == it.room &&

@@ -24,6 +24,7 @@ struct TailLaunch {
     const uint64_t *offset_ptr;   // if set, the call offset is read here (captured graphs)
     int noise_kind;          // 0 logistic (reference), 1 Gaussian (Box-Muller)
     float *env_out;          // optional [n_rir][3]: A, alpha, tau_dp
+    const unsigned char *pre;   // optional [rir]: 1 = silent tail written elsewhere (TailArgs::pre)
 };
 
 __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
@@ -70,6 +71,7 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
         }
     }
     __syncthreads();
+    if (P.pre && P.pre[it.rir]) return;   // silent (A = 0 above) and streamed by the caller
     const uint64_t offset = P.offset_ptr ? *P.offset_ptr : P.offset;
     tail_fill(row + n_ism, n_diff, s0, s0 + kTailChunk, threadIdx.x, kTailThreads, envA, envB, P.seed,
               offset, (uint32_t)it.rir, P.noise_kind);
@@ -78,13 +80,14 @@ __global__ void __launch_bounds__(kTailThreads) tail_kernel(TailLaunch P) {
 cudaError_t tail_launch(const RoomDesc *rooms, const IsmItem *rirs, int n_rir, int max_n_diff,
                         const float *pos_src, const float *pos_rcv, float *out, uint64_t seed,
                         uint64_t offset, const uint64_t *offset_ptr, int noise_kind, float *env_out,
-                        cudaStream_t st) {
+                        cudaStream_t st, const unsigned char *pre) {
     if (n_rir <= 0 || max_n_diff <= 0) return cudaSuccess;
     TailLaunch p;
     p.rooms = rooms; p.rirs = rirs; p.n_rir = n_rir;
     p.pos_src = pos_src; p.pos_rcv = pos_rcv; p.out = out;
     p.seed = seed; p.offset = offset; p.offset_ptr = offset_ptr; p.noise_kind = noise_kind;
     p.env_out = env_out;
+    p.pre = pre;
     const long chunks = ((long)max_n_diff + kTailChunk - 1) / kTailChunk;
     if (chunks > 65535) return cudaErrorInvalidValue;
     dim3 grid(n_rir, (unsigned)chunks);
