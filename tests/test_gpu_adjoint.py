@@ -170,7 +170,7 @@ def test_inverse_problem_recovers_walls(built):
             beta.clamp_(0.05, 0.999)
         first = first if first is not None else float(loss.detach())
     assert float(loss.detach()) < 0.05 * first
-    assert float((beta - true).abs().max()) < float((0.8 - true).abs().max())
+    assert float((beta.detach() - true).abs().max()) < float((0.8 - true).abs().max())
 
 
 def test_device_beta_forward_matches_host_tables(built):
