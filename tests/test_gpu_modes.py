@@ -109,3 +109,26 @@ def test_compensated_accumulation_on_long_dense_rirs(built):
     assert lut_long <= 1.3 * lut_short
     assert lut_long < lut_long_plain
     assert mp_long <= 1.2 * mp_short
+
+
+@pytest.mark.parametrize("mode", ["lut", "mp"])
+def test_image_exactly_on_sample_in_each_mode(built, mode):
+    """Direct path of exactly 50 samples (c = 320 m/s, fs = 16 kHz, 1 m apart): in
+    lookup-table mode the taps at |t - tau| = Tw/2 stay outside the support."""
+    import gpurir_gb300 as G
+    room = np.array([4.0, 4.0, 3.0], np.float32)
+    ps = np.array([[1.0, 2.0, 1.5]], dtype=np.float32)
+    pr = np.array([[2.0, 2.0, 1.5]], dtype=np.float32)
+    nb, T, fs, c = (3, 3, 3), 0.05, 16000.0, 320.0
+    sim = G.Simulator()
+    assert (sim.activate_lut(True) if mode == "lut" else sim.activate_mixed_precision(True))
+    out = sim.simulate_rir(room, [0.7] * 6, ps, pr, None, None, 0, 0, nb, T, T, fs, c=c)
+    amp, tau, _ = oracle.amp_tau(room, [0.7] * 6, ps, pr, nb, fs, c=c)
+    assert abs(tau.reshape(-1)[np.argmin(tau)] - 50.0) < 1e-9
+    n = oracle.n_samples(T, fs)
+    exact = oracle.ism_sum(amp.reshape(1, -1), tau.reshape(1, -1), n, fs)
+    if mode == "lut":
+        lut = oracle.ism_sum_lut(amp.reshape(1, -1), tau.reshape(1, -1), n, fs)
+        assert rel_l2(out.reshape(1, -1), lut) <= 1e-5
+    else:
+        assert rel_l2(out.reshape(1, -1), exact) <= 2e-3
