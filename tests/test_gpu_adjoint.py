@@ -335,7 +335,7 @@ def test_fused_l2_step_matches_composed_step(built):
     loss_f.backward()
     for a, x in zip(comp, params):
         assert torch.equal(a, x.grad)
-    assert abs(float(loss_f) - float(loss_c)) <= 1e-5 * float(loss_c)
+    assert abs(float(loss_f.detach()) - float(loss_c.detach())) <= 1e-5 * float(loss_c.detach())
     assert torch.equal(model.last_rirs, model(beta, ps, pr, None, orv).detach())
     # the graph-free step overwrites .grad with the same values
     loss_s = model.l2_step(beta, ps, pr, None, orv, target)
