@@ -597,7 +597,6 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                         sub_start[s] = st2[h];
                         sub_cnt[s] = cnt2[h];
                         pool_base[s] = epre[h];
-                        for (int w = 0; w < kWarps; w++) hist[w * kMaxSub + s] += st2[h];
                         for (int k = 0; k < full2[h]; k++) order[fpre[h] + k] = s | (k << 8);
                         if (rem2[h] > 0) order[n_full + rk[h]] = s | (full2[h] << 8);
                         for (int k = 0; k < ext2[h]; k++) slot_sub[epre[h] + k] = s;
@@ -627,7 +626,8 @@ __global__ void __launch_bounds__(kThreads, 2) ism_forward_kernel(IsmLaunch P) {
                     dst[r] = -1;
                     if (rel != kNoImage) {   // the sub-range as pass 1 derived it from rel
                         const int sub = rel < 0 ? 0 : min(rel / SUB, nsub - 1);
-                        dst[r] = my_hist[sub] + rec_rank[local];
+                        // sub-range start + this warp's offset in it + rank among its images
+                        dst[r] = sub_start[sub] + my_hist[sub] + rec_rank[local];
                     }
                 }
                 __syncthreads();
